@@ -1,0 +1,367 @@
+"""Benchmark: GPU-Quicksort on GB300, one JSON line.
+
+Default workload (the metric's configuration): one plain sort of 2^28 uint32 keys drawn
+uniformly over [0, 2^32) from a fixed seed. A step is one sort of that array.
+
+  value     keys/s with the keys already in HBM (device-pointer C ABI call, CUDA events around
+            each sort on the launching stream; the input is restored between steps outside the
+            timed interval; 1 GiB of keys exceeds the 129 MB L2, and the restore copy rewrites it)
+  e2e       the same metric through the host-pointer C ABI call (pinned host buffer -> HBM,
+            sort, -> host), wall clock per call
+  roofline  algorithmic bytes of the persistent kernel (key bytes * 2 * keys read by partition
+            chunks + keys sorted on chip + keys sorted in registers, from the kernel's own
+            counters) / its CUDA-event duration, against the measured HBM copy bandwidth
+
+Options: --impl reference times the reference's CPU path (the oracle's restatement of
+GPUQSort<T>, all host threads) on a bounded sample; --config batched runs the segmented form.
+Multi-GPU (torchrun): every rank sorts its own array (replicas; no collective on the data path).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import platform
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "gpu-quicksort_gb300")
+sys.path.insert(0, PKG)
+
+SEED = 20260301
+L2_BYTES = 129 * 1024 * 1024
+
+METRIC = "Gkeys/s @2^28 u32"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--config", default="plain", choices=["plain", "batched"])
+    p.add_argument("--dtype", default="u32", choices=["u32", "f32", "f64"])
+    p.add_argument("--dist", default="uniform")
+    p.add_argument("--log2n", type=int, default=28)
+    p.add_argument("--variant", type=int, default=-1)
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--no-clocks", action="store_true")
+    return p.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def workload_name(args, n):
+    if args.config == "batched":
+        return f"batched segmented sort: 4096 uint32 arrays, lengths log-uniform in [32, 2^20], {n} keys"
+    return f"plain sort, 2^{args.log2n} {args.dtype} keys, {args.dist}"
+
+
+def measured_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            pk = json.load(f)
+        return float(pk["hbm_gbs"]), "measured (MEASURED_PEAKS.json hbm_gbs)"
+    except Exception:
+        return 6800.0, "fallback 6.8 TB/s"
+
+
+def ncu_traffic(workload_key):
+    """Per-launch DRAM bytes of the persistent kernel from a committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return d.get(workload_key)
+    except Exception:
+        return None
+
+
+class ClockSampler:
+    def __init__(self, enabled, index=0):
+        self.proc = None
+        self.path = None
+        if not enabled:
+            return
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        os.makedirs(os.path.join(ROOT, "gpurun_out"), exist_ok=True)
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_bench_{os.getpid()}.csv")
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={index}", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                          "-lms", "100"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    sm.append(float(parts[1]))
+                    mx.append(float(parts[2]))
+                except ValueError:
+                    continue
+                for nm, v in zip(names, parts[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_baseline(args, n_full):
+    """The oracle's restatement of GPUQSort<T> on all host threads, on a bounded sample."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import gqs_ctypes
+    import oracle_ctypes
+    threads = os.cpu_count() or 1
+    ns = min(n_full, 1 << 25)
+    a = gqs_ctypes.generate(args.dtype, args.dist, SEED, ns)
+    b = a.copy()
+    t0 = time.perf_counter()
+    oracle_ctypes.gpuqsort(b, threads=threads)
+    t = time.perf_counter() - t0
+    # the reference's own CPU baseline, std::sort on one core, on a smaller sample
+    ns1 = min(n_full, 1 << 24)
+    c = a[:ns1].copy()
+    t1 = time.perf_counter()
+    oracle_ctypes.std_sort(c)
+    t_std = time.perf_counter() - t1
+    return {"value": ns / t / 1e9, "unit": "Gkeys/s", "cores": threads, "kind": "port",
+            "sample": f"GPUQSort<T> restatement (oracle/gqs_oracle.cpp) on {ns} {args.dtype} keys of the same "
+                      f"distribution, {threads} threads, one sort of {t:.3f} s",
+            "std_sort_1core": {"value": ns1 / t_std / 1e9, "unit": "Gkeys/s", "keys": ns1},
+            "cpu": platform.processor() or platform.machine()}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import gqs_ctypes
+    import oracle_ctypes
+    threads = os.cpu_count() or 1
+    n_full = 1 << args.log2n
+    ns = min(n_full, 1 << 24)
+    a = gqs_ctypes.generate(args.dtype, args.dist, SEED, ns)
+    for _ in range(args.warmup):
+        b = a.copy()
+        oracle_ctypes.gpuqsort(b, threads=threads)
+    times = []
+    for _ in range(args.steps):
+        b = a.copy()
+        t0 = time.perf_counter()
+        oracle_ctypes.gpuqsort(b, threads=threads)
+        times.append(time.perf_counter() - t0)
+    v = ns * len(times) / sum(times) / 1e9
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "Gkeys/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": args.dtype,
+            "data": "synthetic (seeded generator, gpu-quicksort_gb300/workload)",
+            "config": {"workload": workload_name(args, n_full), "sample_keys": ns},
+            "cpu_baseline": {"value": v, "unit": "Gkeys/s", "cores": threads, "kind": "port",
+                             "sample": f"{ns} keys per step (bounded sample of the 2^{args.log2n} workload), "
+                                       "oracle restatement of GPUQSort<T>, all host threads"},
+            "e2e": {"value": v, "unit": "Gkeys/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    import torch
+    import gqs_ctypes
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    else:
+        dist = None
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    tdt = {"u32": torch.int32, "f32": torch.float32, "f64": torch.float64}[args.dtype]
+    npdt = gqs_ctypes.NP_DTYPES[args.dtype]
+    esize = np.dtype(npdt).itemsize
+
+    # ---- input
+    offsets = None
+    if args.config == "batched":
+        off = gqs_ctypes.segment_offsets(SEED + rank, 4096, 32, 1 << 20)
+        n = int(off[-1])
+        offsets = torch.from_numpy(off.astype(np.int64)).cuda()
+    else:
+        n = 1 << args.log2n
+    host_in = torch.empty(n, dtype=tdt, pin_memory=True)
+    hv = host_in.numpy().view(npdt) if args.dtype == "u32" else host_in.numpy()
+    gqs_ctypes.generate(args.dtype, args.dist if args.config == "plain" else "uniform", SEED + rank, n, out=hv)
+    pristine = host_in.cuda()
+    d = torch.empty_like(pristine)
+    dn = torch.empty_like(pristine)
+
+    ctx = gqs_ctypes.Context(device=local, sync=False, timing=True, variant=args.variant)
+    stream = torch.cuda.current_stream()
+
+    def sort_once():
+        if offsets is None:
+            rc = ctx.sort_dev(args.dtype, d.data_ptr(), dn.data_ptr(), n, stream.cuda_stream)
+        else:
+            rc = ctx.sort_segments_dev(args.dtype, d.data_ptr(), dn.data_ptr(), n, offsets.data_ptr(), 4096,
+                                       stream.cuda_stream)
+        if rc != 0:
+            raise RuntimeError(f"sort enqueue failed: {gqs_ctypes.STATUS.get(rc, rc)}")
+
+    for _ in range(args.warmup):
+        d.copy_(pristine)
+        sort_once()
+        st = ctx.stats()
+        if st["status"] != 0:
+            raise RuntimeError(f"sort failed: {st}")
+    torch.cuda.synchronize()
+
+    # correctness of the warm-up result (outside any timed interval)
+    check = {}
+    if offsets is None:
+        if args.dtype == "u32":
+            got = d.to(torch.int64) & 0xFFFFFFFF
+            ref = torch.sort(pristine.to(torch.int64) & 0xFFFFFFFF).values
+        else:
+            got, ref = d, torch.sort(pristine).values
+        check["bit_exact_vs_torch_sort"] = bool(torch.equal(got, ref))
+        del got, ref
+    torch.cuda.empty_cache()
+
+    clocks = ClockSampler(enabled=(not args.no_clocks and rank == 0), index=local)
+    ev0 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ev1 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    kernel_ms, algo_bytes, stats_last = [], [], None
+    barrier()
+    torch.cuda.synchronize()
+    wall0 = time.perf_counter()
+    for i in range(args.steps):
+        d.copy_(pristine)
+        ev0[i].record(stream)
+        sort_once()
+        ev1[i].record(stream)
+        st = ctx.stats()  # waits for this sort; kernel time from events on the launching stream
+        if st["status"] != 0:
+            raise RuntimeError(f"sort failed: {st}")
+        kernel_ms.append(st["kernel_ms"])
+        algo_bytes.append(st["algo_bytes"])
+        stats_last = st
+    torch.cuda.synchronize()
+    barrier()
+    wall = time.perf_counter() - wall0
+    clk = clocks.stop()
+    step_ms = [a.elapsed_time(b) for a, b in zip(ev0, ev1)]
+    t_sort = sum(step_ms) / 1e3
+    if dist is not None:
+        tt = torch.tensor([t_sort], dtype=torch.float64, device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_sort = float(tt.item())
+    value = n * world * args.steps / t_sort / 1e9
+
+    # ---- end to end through the host-pointer call
+    e2e = None
+    if not args.no_e2e and offsets is None:
+        work = torch.empty_like(host_in, pin_memory=True)
+        wv = work.numpy().view(npdt) if args.dtype == "u32" else work.numpy()
+        for _ in range(max(1, min(args.warmup, 2))):
+            work.copy_(host_in)
+            ctx.sort(wv)
+        times = []
+        for _ in range(args.steps):
+            work.copy_(host_in)
+            t0 = time.perf_counter()
+            ctx.sort(wv)
+            times.append(time.perf_counter() - t0)
+        tsum = sum(times)
+        if dist is not None:
+            tt = torch.tensor([tsum], dtype=torch.float64, device="cuda")
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            tsum = float(tt.item())
+        e2e = {"value": n * world * args.steps / tsum / 1e9, "unit": "Gkeys/s",
+               "h2d_bytes_per_step": n * esize, "d2h_bytes_per_step": n * esize,
+               "ms_per_step": 1e3 * tsum / args.steps, "api": "gqs_sort_" + args.dtype + " (host pointers, pinned)"}
+
+    if rank != 0:
+        ctx.close()
+        if dist is not None:
+            dist.destroy_process_group()
+        return
+
+    peak, peak_src = measured_peak()
+    km = float(np.mean(kernel_ms))
+    ab = float(np.mean(algo_bytes))
+    achieved = ab / (km / 1e3) / 1e9
+    wkey = f"plain_{args.dtype}_{args.dist}_2^{args.log2n}" if offsets is None else "batched_u32_4096"
+    traffic = ncu_traffic(wkey)
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": traffic, "kernel": "gqs::persistent_kernel", "kernel_ms": km,
+                "algo_bytes_per_launch": ab, "peak_source": peak_src,
+                "per_unit": f"{esize} B x 2 per key per pass (partition chunks + on-chip sort + register sort)"}
+    cpu = None if args.no_cpu else cpu_baseline(args, n)
+    v0 = gqs_ctypes.variants(args.dtype)[stats_last["variant"]]
+    line = {
+        "metric": METRIC if (args.config == "plain" and args.log2n == 28 and args.dtype == "u32")
+        else f"Gkeys/s ({workload_name(args, n)})",
+        "value": value, "unit": "Gkeys/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * t_sort / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": args.dtype, "data": "synthetic (seeded generator, gpu-quicksort_gb300/workload)",
+        "config": {"workload": workload_name(args, n), "keys": n, "distribution": args.dist, "seed": SEED,
+                   "l2": "inputs larger than L2 (keys rewritten from a pristine copy before every step)",
+                   "variant": v0["name"], "grid": stats_last["grid"], "threads": stats_last["threads"],
+                   "parallelism": f"replicas x{world}"},
+        "roofline": roofline,
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "gpu_launches": 2 * args.steps,
+        "clocks": clk,
+        "check": check,
+        "stats": {k: stats_last[k] for k in ("part_keys", "local_keys", "tiny_keys", "fill_keys", "chunks",
+                                             "part_jobs", "local_jobs", "fill_chunks", "max_depth")},
+        "passes_per_key": (stats_last["part_keys"] + stats_last["local_keys"] + stats_last["tiny_keys"]) / n,
+        "wall_s": wall,
+    }
+    print(json.dumps(line), flush=True)
+    ctx.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

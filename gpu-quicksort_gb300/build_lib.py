@@ -1,0 +1,91 @@
+"""Builds the gqs shared libraries in-tree (no cmake, no pip).
+
+    libgqs.so           the CUDA sort library behind include/gqs.h (sm_103a only)
+    libgqs_workload.so  seeded synthetic workload generators (host C++)
+
+Objects go to _build/ next to this file; the libraries land beside this file.
+Run as a script or call build().
+"""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+CSRC = os.path.join(HERE, "csrc")
+BUILD = os.path.join(HERE, "_build")
+INCLUDE = os.path.join(ROOT, "include")
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
+              "--expt-relaxed-constexpr", "-I" + CSRC, "-I" + INCLUDE]
+CU_SOURCES = ["gqs_sort_u32.cu", "gqs_sort_f32.cu", "gqs_sort_f64.cu", "gqs_capi.cu"]
+
+LIB = os.path.join(HERE, "libgqs.so")
+WORKLOAD_LIB = os.path.join(HERE, "libgqs_workload.so")
+
+
+def _nvcc() -> str:
+    for cand in (shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
+        if cand and os.path.exists(cand):
+            return cand
+    raise RuntimeError("nvcc not found")
+
+
+def _run(cmd: list[str]) -> None:
+    r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("build step failed:\n" + " ".join(cmd) + "\n" + r.stdout)
+
+
+def _stale(target: str, deps: list[str]) -> bool:
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    return any(os.path.getmtime(d) > t for d in deps)
+
+
+def _headers() -> list[str]:
+    hs = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
+    hs.append(os.path.join(INCLUDE, "gqs.h"))
+    return hs
+
+
+def build(force: bool = False, verbose: bool = False) -> dict:
+    """Compiles what is out of date; returns the library paths."""
+    os.makedirs(BUILD, exist_ok=True)
+    nvcc = _nvcc()
+    headers = _headers()
+    jobs = []
+    objs = []
+    for src in CU_SOURCES:
+        s = os.path.join(CSRC, src)
+        o = os.path.join(BUILD, src.replace(".cu", ".o"))
+        objs.append(o)
+        if force or _stale(o, [s] + headers):
+            jobs.append([nvcc] + ARCH + NVCC_FLAGS + ["-c", s, "-o", o])
+    wsrc = os.path.join(HERE, "workload", "gqs_workload.cpp")
+    whdr = os.path.join(HERE, "workload", "gqs_workload.h")
+    wjob = None
+    if force or _stale(WORKLOAD_LIB, [wsrc, whdr]):
+        wjob = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off",
+                "-fno-fast-math", "-I" + os.path.join(HERE, "workload"), wsrc, "-o", WORKLOAD_LIB]
+    with cf.ThreadPoolExecutor(max_workers=max(1, min(8, os.cpu_count() or 1))) as ex:
+        futs = [ex.submit(_run, j) for j in jobs]
+        if wjob:
+            futs.append(ex.submit(_run, wjob))
+        for f in futs:
+            f.result()
+    if force or jobs or _stale(LIB, objs):
+        _run([nvcc] + ARCH + ["-shared", "-o", LIB] + objs + ["-Xcompiler", "-fPIC"])
+    if verbose:
+        print("built", LIB, WORKLOAD_LIB)
+    return {"lib": LIB, "workload": WORKLOAD_LIB}
+
+
+if __name__ == "__main__":
+    build(force="--force" in sys.argv, verbose=True)

@@ -1,0 +1,539 @@
+// The C ABI (include/gqs.h): contexts, pools, argument checks, launches, status and stats.
+//
+// Host-side replacement for the reference's GPUQSort<T> driver
+// (GPU-Quicksort_Full_SYCL/QuicksortMain.cpp:835-906). The reference rebuilds its records on the
+// host and reads results back after every partition level (QuicksortMain.cpp:858-899); here one
+// seed launch and one persistent launch sort the whole array, and the host only reads a small
+// status block at the end.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdint>
+#include <cstring>
+#include <mutex>
+#include <new>
+
+#include "gqs.h"
+#include "gqs_device.cuh"
+#include "gqs_launch.h"
+
+namespace gqs {
+
+int variant_count(int dtype) {
+  switch (dtype) {
+    case DT_U32: return variant_count_u32();
+    case DT_F32: return variant_count_f32();
+    case DT_F64: return variant_count_f64();
+    default: return 0;
+  }
+}
+VariantInfo variant_info(int dtype, int v) {
+  switch (dtype) {
+    case DT_U32: return variant_info_u32(v);
+    case DT_F32: return variant_info_f32(v);
+    default: return variant_info_f64(v);
+  }
+}
+int variant_prepare(int dtype, int v) {
+  switch (dtype) {
+    case DT_U32: return variant_prepare_u32(v);
+    case DT_F32: return variant_prepare_f32(v);
+    default: return variant_prepare_f64(v);
+  }
+}
+cudaError_t launch_sort(int dtype, const LaunchParams& p) {
+  switch (dtype) {
+    case DT_U32: return launch_u32(p);
+    case DT_F32: return launch_f32(p);
+    default: return launch_f64(p);
+  }
+}
+
+}  // namespace gqs
+
+namespace {
+
+constexpr int kMaxVariants = 16;
+constexpr size_t kElemSize[3] = {4, 4, 8};
+
+struct DeviceGuard {
+  int prev = -1;
+  explicit DeviceGuard(int dev) {
+    if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+    if (prev != dev) cudaSetDevice(dev);
+  }
+  ~DeviceGuard() {
+    int cur = -1;
+    if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+  }
+};
+
+}  // namespace
+
+struct gqs_ctx {
+  int device = 0;
+  int num_sms = 0;
+  gqs_config cfg{};
+  std::mutex mu;
+  cudaStream_t stream = nullptr;  // used by the host-pointer calls
+  void* pool_d = nullptr;
+  size_t pool_d_bytes = 0;
+  void* pool_dn = nullptr;
+  size_t pool_dn_bytes = 0;
+  gqs::Job* jobs = nullptr;
+  size_t job_cap = 0;
+  gqs::Queue* q = nullptr;
+  gqs::Queue* q_host = nullptr;  // pinned
+  unsigned long long* offs = nullptr;
+  size_t offs_cap = 0;
+  uint32_t epoch = 0;
+  cudaEvent_t ev_begin = nullptr, ev_end = nullptr, ev_done = nullptr;
+  bool pending = false;
+  bool pending_timed = false;
+  int pending_dtype = 0;
+  int pending_variant = 0;
+  int pending_grid = 0;
+  unsigned long long pending_keys = 0;
+  gqs_stats last{};
+  int variant[3] = {0, 0, 0};
+  int blocks_per_sm[3][kMaxVariants] = {};
+};
+
+namespace {
+
+gqs_status cuda_status(cudaError_t e) {
+  if (e == cudaSuccess) return GQS_OK;
+  if (e == cudaErrorMemoryAllocation) return GQS_ERR_NOMEM;
+  return GQS_ERR_CUDA;
+}
+
+// Grows a device buffer to at least `bytes`; callers have waited for pending work.
+gqs_status grow(void** p, size_t* cap, size_t bytes) {
+  if (*cap >= bytes && *p) return GQS_OK;
+  if (*p) cudaFree(*p);
+  *p = nullptr;
+  *cap = 0;
+  size_t want = std::max(bytes, (size_t)256);
+  cudaError_t e = cudaMalloc(p, want);
+  if (e != cudaSuccess) {
+    *p = nullptr;
+    (void)cudaGetLastError();
+    return GQS_ERR_NOMEM;
+  }
+  *cap = want;
+  return GQS_OK;
+}
+
+// Job records one sort can need: local jobs are disjoint ranges longer than `tiny` keys,
+// partition jobs ranges longer than `tile` keys (with generous room for uneven pivots), plus
+// one root per segment and the fill jobs of long pivot runs.
+size_t job_capacity(const gqs::VariantInfo& vi, size_t n, size_t nseg) {
+  return n / (size_t)vi.tiny + 16 * (n / (size_t)vi.tile) + n / 32768 + 2 * nseg + 4096;
+}
+
+gqs_status wait_pending_locked(gqs_ctx* c) {
+  if (!c->pending) return GQS_OK;
+  cudaError_t e = cudaEventSynchronize(c->ev_done);
+  if (e != cudaSuccess) return cuda_status(e);
+  e = cudaMemcpy(c->q_host, c->q, sizeof(gqs::Queue), cudaMemcpyDeviceToHost);
+  c->pending = false;
+  if (e != cudaSuccess) return cuda_status(e);
+  const gqs::Queue& q = *c->q_host;
+  gqs_stats s{};
+  s.keys = q.total;
+  s.part_keys = q.part_keys;
+  s.local_keys = q.local_keys;
+  s.tiny_keys = q.tiny_keys;
+  s.fill_keys = q.fill_keys;
+  s.chunks = q.chunks;
+  s.algo_bytes = kElemSize[c->pending_dtype] * 2 * (q.part_keys + q.local_keys + q.tiny_keys);
+  s.part_jobs = q.part_jobs;
+  s.local_jobs = q.local_jobs;
+  s.fill_chunks = q.fill_jobs;
+  s.max_depth = q.max_depth;
+  s.status = q.error;
+  s.variant = (uint32_t)c->pending_variant;
+  s.grid = (uint32_t)c->pending_grid;
+  s.threads = (uint32_t)gqs::variant_info(c->pending_dtype, c->pending_variant).threads;
+  s.kernel_ms = -1.0;
+  if (c->pending_timed) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, c->ev_begin, c->ev_end) == cudaSuccess) s.kernel_ms = ms;
+  }
+  if (q.error == 0 && q.done != q.total) s.status = GQS_ERR_INTERNAL;
+  c->last = s;
+  return (gqs_status)s.status;
+}
+
+// Validates, grows pools, and enqueues one sort on `stream`. Caller holds the lock.
+gqs_status enqueue_locked(gqs_ctx* c, int dtype, void* d, void* dn, size_t n, const unsigned long long* offsets,
+                          size_t nseg, cudaStream_t stream) {
+  const size_t es = kElemSize[dtype];
+  if (!d || (reinterpret_cast<uintptr_t>(d) % es) != 0) return GQS_ERR_INVALID;
+  if (dn && (reinterpret_cast<uintptr_t>(dn) % es) != 0) return GQS_ERR_INVALID;
+  if (n >= (1ull << 40) || nseg >= (1ull << 31)) return GQS_ERR_INVALID;
+  const int v = c->variant[dtype];
+  const gqs::VariantInfo vi = gqs::variant_info(dtype, v);
+  const size_t cap = job_capacity(vi, n, nseg);
+  if (cap >= (1ull << 32)) return GQS_ERR_INVALID;
+  if (!c->blocks_per_sm[dtype][v]) {
+    c->blocks_per_sm[dtype][v] = gqs::variant_prepare(dtype, v);
+    if (!c->blocks_per_sm[dtype][v]) return GQS_ERR_NO_DEVICE;
+  }
+  gqs_status st = GQS_OK;
+  const bool need_jobs = c->job_cap < cap;
+  const bool need_dn = !dn && c->pool_dn_bytes < n * es;
+  if (need_jobs || need_dn) {
+    st = wait_pending_locked(c);
+    if (st != GQS_OK && st != GQS_ERR_TIMEOUT && st != GQS_ERR_CAPACITY && st != GQS_ERR_INTERNAL) return st;
+    size_t bytes = 0;
+    if (need_jobs) {
+      void* p = c->jobs;
+      bytes = c->job_cap * sizeof(gqs::Job);
+      st = grow(&p, &bytes, cap * sizeof(gqs::Job));
+      c->jobs = static_cast<gqs::Job*>(p);
+      c->job_cap = c->jobs ? bytes / sizeof(gqs::Job) : 0;
+      if (st != GQS_OK) return st;
+      // fresh records must not carry a stale epoch
+      cudaError_t e = cudaMemset(c->jobs, 0, c->job_cap * sizeof(gqs::Job));
+      if (e != cudaSuccess) return cuda_status(e);
+    }
+    if (need_dn) {
+      st = grow(&c->pool_dn, &c->pool_dn_bytes, n * es);
+      if (st != GQS_OK) return st;
+    }
+  }
+  if (!dn) dn = c->pool_dn;
+  if (c->pending) {
+    cudaError_t e = cudaStreamWaitEvent(stream, c->ev_done, 0);
+    if (e != cudaSuccess) return cuda_status(e);
+  }
+  cudaError_t e = cudaMemsetAsync(c->q, 0, sizeof(gqs::Queue), stream);
+  if (e != cudaSuccess) return cuda_status(e);
+  if (++c->epoch == 0) {
+    c->epoch = 1;
+    e = cudaMemsetAsync(c->jobs, 0, c->job_cap * sizeof(gqs::Job), stream);
+    if (e != cudaSuccess) return cuda_status(e);
+  }
+  gqs::LaunchParams p{};
+  p.d = d;
+  p.dn = dn;
+  p.jobs = c->jobs;
+  p.q = c->q;
+  p.capacity = (uint32_t)c->job_cap;
+  p.epoch = c->epoch;
+  p.timeout_ns = (unsigned long long)(c->cfg.timeout_ms ? c->cfg.timeout_ms : 4000) * 1000000ull;
+  p.offsets = offsets;
+  p.n = n;
+  p.nseg = (uint32_t)(offsets ? nseg : 1);
+  p.variant = v;
+  p.grid = c->num_sms * c->blocks_per_sm[dtype][v];
+  p.stream = stream;
+  p.ev_begin = c->cfg.timing ? c->ev_begin : nullptr;
+  p.ev_end = c->cfg.timing ? c->ev_end : nullptr;
+  e = gqs::launch_sort(dtype, p);
+  if (e != cudaSuccess) return cuda_status(e);
+  e = cudaEventRecord(c->ev_done, stream);
+  if (e != cudaSuccess) return cuda_status(e);
+  c->pending = true;
+  c->pending_timed = c->cfg.timing != 0;
+  c->pending_dtype = dtype;
+  c->pending_variant = v;
+  c->pending_grid = p.grid;
+  c->pending_keys = offsets ? 0 : n;
+  return GQS_OK;
+}
+
+gqs_status sort_dev(gqs_ctx* c, int dtype, void* d, void* scratch, size_t n, void* stream) {
+  if (!c) return GQS_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(c->mu);
+  DeviceGuard dg(c->device);
+  if (n <= 1) return d || n == 0 ? GQS_OK : GQS_ERR_INVALID;
+  gqs_status st = enqueue_locked(c, dtype, d, scratch, n, nullptr, 1, static_cast<cudaStream_t>(stream));
+  if (st != GQS_OK) return st;
+  if (c->cfg.sync) return wait_pending_locked(c);
+  return GQS_OK;
+}
+
+gqs_status sort_host(gqs_ctx* c, int dtype, void* d, size_t n) {
+  if (!c) return GQS_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(c->mu);
+  DeviceGuard dg(c->device);
+  if (n <= 1) return d || n == 0 ? GQS_OK : GQS_ERR_INVALID;
+  if (!d) return GQS_ERR_INVALID;
+  const size_t bytes = n * kElemSize[dtype];
+  if (c->pool_d_bytes < bytes) {
+    gqs_status st = wait_pending_locked(c);
+    (void)st;
+    st = grow(&c->pool_d, &c->pool_d_bytes, bytes);
+    if (st != GQS_OK) return st;
+  }
+  cudaError_t e = cudaMemcpyAsync(c->pool_d, d, bytes, cudaMemcpyHostToDevice, c->stream);
+  if (e != cudaSuccess) return cuda_status(e);
+  gqs_status st = enqueue_locked(c, dtype, c->pool_d, nullptr, n, nullptr, 1, c->stream);
+  if (st != GQS_OK) return st;
+  e = cudaMemcpyAsync(d, c->pool_d, bytes, cudaMemcpyDeviceToHost, c->stream);
+  if (e != cudaSuccess) return cuda_status(e);
+  e = cudaEventRecord(c->ev_done, c->stream);
+  if (e != cudaSuccess) return cuda_status(e);
+  return wait_pending_locked(c);
+}
+
+gqs_status sort_segments_dev(gqs_ctx* c, int dtype, void* keys, void* scratch, size_t n, const uint64_t* offsets,
+                             size_t nseg, void* stream) {
+  if (!c) return GQS_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(c->mu);
+  DeviceGuard dg(c->device);
+  if (nseg == 0) return GQS_OK;
+  if (!offsets || !keys) return GQS_ERR_INVALID;
+  gqs_status st = enqueue_locked(c, dtype, keys, scratch, n, reinterpret_cast<const unsigned long long*>(offsets),
+                                 nseg, static_cast<cudaStream_t>(stream));
+  if (st != GQS_OK) return st;
+  if (c->cfg.sync) return wait_pending_locked(c);
+  return GQS_OK;
+}
+
+gqs_status sort_segments_host(gqs_ctx* c, int dtype, void* keys, size_t n, const uint64_t* offsets, size_t nseg) {
+  if (!c) return GQS_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(c->mu);
+  DeviceGuard dg(c->device);
+  if (nseg == 0) return GQS_OK;
+  if (!offsets || (!keys && n)) return GQS_ERR_INVALID;
+  for (size_t i = 0; i < nseg; ++i)
+    if (offsets[i + 1] < offsets[i]) return GQS_ERR_INVALID;
+  if (offsets[nseg] > n || offsets[0] > offsets[nseg]) return GQS_ERR_INVALID;
+  if (n == 0) return GQS_OK;
+  const size_t bytes = n * kElemSize[dtype];
+  const size_t obytes = (nseg + 1) * sizeof(uint64_t);
+  if (c->pool_d_bytes < bytes || c->offs_cap < obytes) {
+    (void)wait_pending_locked(c);
+    gqs_status st = grow(&c->pool_d, &c->pool_d_bytes, bytes);
+    if (st != GQS_OK) return st;
+    void* po = c->offs;
+    st = grow(&po, &c->offs_cap, obytes);
+    c->offs = static_cast<unsigned long long*>(po);
+    if (st != GQS_OK) return st;
+  }
+  cudaError_t e = cudaMemcpyAsync(c->pool_d, keys, bytes, cudaMemcpyHostToDevice, c->stream);
+  if (e != cudaSuccess) return cuda_status(e);
+  e = cudaMemcpyAsync(c->offs, offsets, obytes, cudaMemcpyHostToDevice, c->stream);
+  if (e != cudaSuccess) return cuda_status(e);
+  gqs_status st = enqueue_locked(c, dtype, c->pool_d, nullptr, n, c->offs, nseg, c->stream);
+  if (st != GQS_OK) return st;
+  e = cudaMemcpyAsync(keys, c->pool_d, bytes, cudaMemcpyDeviceToHost, c->stream);
+  if (e != cudaSuccess) return cuda_status(e);
+  e = cudaEventRecord(c->ev_done, c->stream);
+  if (e != cudaSuccess) return cuda_status(e);
+  return wait_pending_locked(c);
+}
+
+}  // namespace
+
+extern "C" {
+
+void gqs_config_default(gqs_config* cfg) {
+  if (!cfg) return;
+  std::memset(cfg, 0, sizeof(*cfg));
+  cfg->variant = -1;
+  cfg->timeout_ms = 4000;
+  cfg->sync = 1;
+  cfg->timing = 0;
+}
+
+gqs_status gqs_create(gqs_ctx** out, int device, const gqs_config* cfg) {
+  if (!out) return GQS_ERR_INVALID;
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) {
+    (void)cudaGetLastError();
+    return GQS_ERR_NO_DEVICE;
+  }
+  if (device < 0 || device >= ndev) return GQS_ERR_INVALID;
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) return GQS_ERR_NO_DEVICE;
+  if (prop.major != 10 || prop.minor != 3) return GQS_ERR_NO_DEVICE;  // built for sm_103a only
+  gqs_ctx* c = new (std::nothrow) gqs_ctx();
+  if (!c) return GQS_ERR_NOMEM;
+  c->device = device;
+  c->num_sms = prop.multiProcessorCount;
+  gqs_config_default(&c->cfg);
+  if (cfg) c->cfg = *cfg;
+  DeviceGuard dg(device);
+  gqs_status st = GQS_OK;
+  do {
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) { st = GQS_ERR_CUDA; break; }
+    if (cudaEventCreate(&c->ev_begin) != cudaSuccess || cudaEventCreate(&c->ev_end) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->ev_done, cudaEventDisableTiming) != cudaSuccess) {
+      st = GQS_ERR_CUDA;
+      break;
+    }
+    if (cudaMalloc(&c->q, sizeof(gqs::Queue)) != cudaSuccess) { st = GQS_ERR_NOMEM; break; }
+    if (cudaMallocHost(&c->q_host, sizeof(gqs::Queue)) != cudaSuccess) { st = GQS_ERR_NOMEM; break; }
+    for (int t = 0; t < 3; ++t) {
+      int v = c->cfg.variant;
+      if (v < 0 || v >= gqs::variant_count(t)) v = 0;
+      c->variant[t] = v;
+    }
+  } while (0);
+  if (st != GQS_OK) {
+    (void)cudaGetLastError();
+    gqs_destroy(c);
+    return st;
+  }
+  *out = c;
+  return GQS_OK;
+}
+
+void gqs_destroy(gqs_ctx* c) {
+  if (!c) return;
+  {
+    DeviceGuard dg(c->device);
+    if (c->pending && c->ev_done) cudaEventSynchronize(c->ev_done);
+    if (c->pool_d) cudaFree(c->pool_d);
+    if (c->pool_dn) cudaFree(c->pool_dn);
+    if (c->jobs) cudaFree(c->jobs);
+    if (c->q) cudaFree(c->q);
+    if (c->offs) cudaFree(c->offs);
+    if (c->q_host) cudaFreeHost(c->q_host);
+    if (c->ev_begin) cudaEventDestroy(c->ev_begin);
+    if (c->ev_end) cudaEventDestroy(c->ev_end);
+    if (c->ev_done) cudaEventDestroy(c->ev_done);
+    if (c->stream) cudaStreamDestroy(c->stream);
+  }
+  delete c;
+}
+
+gqs_status gqs_reserve(gqs_ctx* c, int dtype, size_t n, size_t nseg, int with_buffers) {
+  if (!c || dtype < 0 || dtype > 2) return GQS_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(c->mu);
+  DeviceGuard dg(c->device);
+  (void)wait_pending_locked(c);
+  const int v = c->variant[dtype];
+  const gqs::VariantInfo vi = gqs::variant_info(dtype, v);
+  if (!c->blocks_per_sm[dtype][v]) {
+    c->blocks_per_sm[dtype][v] = gqs::variant_prepare(dtype, v);
+    if (!c->blocks_per_sm[dtype][v]) return GQS_ERR_NO_DEVICE;
+  }
+  const size_t cap = job_capacity(vi, n, nseg ? nseg : 1);
+  if (c->job_cap < cap) {
+    void* p = c->jobs;
+    size_t bytes = c->job_cap * sizeof(gqs::Job);
+    gqs_status st = grow(&p, &bytes, cap * sizeof(gqs::Job));
+    c->jobs = static_cast<gqs::Job*>(p);
+    c->job_cap = c->jobs ? bytes / sizeof(gqs::Job) : 0;
+    if (st != GQS_OK) return st;
+    if (cudaMemset(c->jobs, 0, c->job_cap * sizeof(gqs::Job)) != cudaSuccess) return GQS_ERR_CUDA;
+  }
+  const size_t bytes = n * kElemSize[dtype];
+  gqs_status st = grow(&c->pool_dn, &c->pool_dn_bytes, bytes);
+  if (st != GQS_OK) return st;
+  if (with_buffers) {
+    st = grow(&c->pool_d, &c->pool_d_bytes, bytes);
+    if (st != GQS_OK) return st;
+    void* po = c->offs;
+    st = grow(&po, &c->offs_cap, ((nseg ? nseg : 1) + 1) * sizeof(uint64_t));
+    c->offs = static_cast<unsigned long long*>(po);
+    if (st != GQS_OK) return st;
+  }
+  return GQS_OK;
+}
+
+gqs_status gqs_sort_u32(gqs_ctx* c, uint32_t* d, uint32_t*, size_t n) { return sort_host(c, gqs::DT_U32, d, n); }
+gqs_status gqs_sort_f32(gqs_ctx* c, float* d, float*, size_t n) { return sort_host(c, gqs::DT_F32, d, n); }
+gqs_status gqs_sort_f64(gqs_ctx* c, double* d, double*, size_t n) { return sort_host(c, gqs::DT_F64, d, n); }
+
+gqs_status gqs_sort_u32_dev(gqs_ctx* c, uint32_t* d, uint32_t* s, size_t n, void* stream) {
+  return sort_dev(c, gqs::DT_U32, d, s, n, stream);
+}
+gqs_status gqs_sort_f32_dev(gqs_ctx* c, float* d, float* s, size_t n, void* stream) {
+  return sort_dev(c, gqs::DT_F32, d, s, n, stream);
+}
+gqs_status gqs_sort_f64_dev(gqs_ctx* c, double* d, double* s, size_t n, void* stream) {
+  return sort_dev(c, gqs::DT_F64, d, s, n, stream);
+}
+
+gqs_status gqs_sort_segments_u32_dev(gqs_ctx* c, uint32_t* k, uint32_t* s, size_t n, const uint64_t* o, size_t ns,
+                                     void* stream) {
+  return sort_segments_dev(c, gqs::DT_U32, k, s, n, o, ns, stream);
+}
+gqs_status gqs_sort_segments_f32_dev(gqs_ctx* c, float* k, float* s, size_t n, const uint64_t* o, size_t ns,
+                                     void* stream) {
+  return sort_segments_dev(c, gqs::DT_F32, k, s, n, o, ns, stream);
+}
+gqs_status gqs_sort_segments_f64_dev(gqs_ctx* c, double* k, double* s, size_t n, const uint64_t* o, size_t ns,
+                                     void* stream) {
+  return sort_segments_dev(c, gqs::DT_F64, k, s, n, o, ns, stream);
+}
+gqs_status gqs_sort_segments_u32(gqs_ctx* c, uint32_t* k, size_t n, const uint64_t* o, size_t ns) {
+  return sort_segments_host(c, gqs::DT_U32, k, n, o, ns);
+}
+gqs_status gqs_sort_segments_f32(gqs_ctx* c, float* k, size_t n, const uint64_t* o, size_t ns) {
+  return sort_segments_host(c, gqs::DT_F32, k, n, o, ns);
+}
+gqs_status gqs_sort_segments_f64(gqs_ctx* c, double* k, size_t n, const uint64_t* o, size_t ns) {
+  return sort_segments_host(c, gqs::DT_F64, k, n, o, ns);
+}
+
+gqs_status gqs_sync(gqs_ctx* c) {
+  if (!c) return GQS_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(c->mu);
+  DeviceGuard dg(c->device);
+  if (!c->pending) return (gqs_status)c->last.status;
+  return wait_pending_locked(c);
+}
+
+gqs_status gqs_last_stats(gqs_ctx* c, gqs_stats* out) {
+  if (!c || !out) return GQS_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(c->mu);
+  DeviceGuard dg(c->device);
+  gqs_status st = wait_pending_locked(c);
+  *out = c->last;
+  return st == GQS_OK ? GQS_OK : st;
+}
+
+int gqs_variant_count(int dtype) { return gqs::variant_count(dtype); }
+
+gqs_status gqs_variant_describe(int dtype, int v, gqs_variant_desc* out) {
+  if (!out || dtype < 0 || dtype > 2 || v < 0 || v >= gqs::variant_count(dtype)) return GQS_ERR_INVALID;
+  const gqs::VariantInfo vi = gqs::variant_info(dtype, v);
+  out->threads = vi.threads;
+  out->tile = vi.tile;
+  out->chunk = vi.chunk;
+  out->kpt = vi.kpt;
+  out->stages = vi.stages;
+  out->tiny = vi.tiny;
+  out->smem_bytes = vi.smem;
+  std::memset(out->name, 0, sizeof(out->name));
+  std::strncpy(out->name, vi.name, sizeof(out->name) - 1);
+  return GQS_OK;
+}
+
+gqs_status gqs_set_variant(gqs_ctx* c, int dtype, int v) {
+  if (!c || dtype < 0 || dtype > 2 || v < 0 || v >= gqs::variant_count(dtype)) return GQS_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(c->mu);
+  c->variant[dtype] = v;
+  return GQS_OK;
+}
+
+int gqs_get_variant(gqs_ctx* c, int dtype) {
+  if (!c || dtype < 0 || dtype > 2) return -1;
+  return c->variant[dtype];
+}
+
+const char* gqs_strerror(gqs_status s) {
+  switch (s) {
+    case GQS_OK: return "ok";
+    case GQS_ERR_INVALID: return "invalid argument";
+    case GQS_ERR_CUDA: return "CUDA runtime error";
+    case GQS_ERR_NOMEM: return "out of memory";
+    case GQS_ERR_TIMEOUT: return "device wait timed out (no progress)";
+    case GQS_ERR_CAPACITY: return "device job queue overflow";
+    case GQS_ERR_NO_DEVICE: return "no sm_103 CUDA device";
+    case GQS_ERR_INTERNAL: return "internal error";
+  }
+  return "unknown status";
+}
+
+int gqs_version(void) { return 1; }
+
+}  // extern "C"

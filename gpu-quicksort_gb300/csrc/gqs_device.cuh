@@ -1,0 +1,1080 @@
+// GPU-Quicksort for sm_103a: one persistent kernel that drains a device-resident
+// queue of partition jobs, so the host never round-trips between levels.
+//
+// Reference mapping (GPU-Quicksort, rioffe/gpu-quicksort):
+//   * partition job  <- gqsort_kernel (GPU-Quicksort_OpenCL_1.2/QuicksortKernels.cl:102-240;
+//                       GPU-Quicksort_Full_SYCL/QuicksortMain.cpp:547-710)
+//   * local job      <- lqsort_kernel (QuicksortKernels.cl:267-421; QuicksortMain.cpp:286-542)
+//   * warp bitonic   <- bitonic_sort / sort_threshold (QuicksortKernels.cl:40-97)
+//   * job queue      <- the host level loop of GPUQSort<T> (QuicksortMain.cpp:835-906) and the
+//                       OpenCL 2.0 device-side relaunch (GPU-Quicksort_OpenCL_2.0/QuicksortKernels.cl:132-222)
+//   * Job            <- work_record / parent_record / block_record (GPU-Quicksort_Full_SYCL/Quicksort.h:145-184)
+//
+// Roles inside one CTA (one CTA per SM):
+//   warps [0, NCW)  consumers: partition staged chunks, run local (on-chip) sorts, fill pivot runs
+//   warp  NCW       producer:  takes work from the global queue and stages it in shared memory with
+//                              bulk TMA copies (cp.async.bulk + mbarrier), STAGES deep
+//   warp  NCW+1     completer: finishes a partition job once its last chunk is written (pivot run,
+//                              child pivots, children pushed back to the queue or sorted in registers)
+//
+// Keys are compared through an order-preserving map to unsigned integers (identity for uint32;
+// for float/double the sign-magnitude bit flip), so every comparison runs on the integer pipes
+// and no float/double compare instruction is issued. Memory always holds the caller's raw bits.
+#pragma once
+#include <cstdint>
+#include "gqs_ptx.cuh"
+
+namespace gqs {
+
+// ---------------------------------------------------------------------------
+// Status codes written by the kernels (the C ABI uses the same numbers).
+enum : uint32_t { ST_OK = 0, ST_INVALID = 1, ST_TIMEOUT = 4, ST_CAPACITY = 5, ST_INTERNAL = 7 };
+
+enum : uint32_t { JOB_PART = 1, JOB_LOCAL = 2, JOB_FILL = 3 };
+enum : uint32_t { ITEM_PART = 1, ITEM_LOCAL = 2, ITEM_FILL = 3, ITEM_TERM = 4, ITEM_FLUSH = 5, ITEM_NONE = 6 };
+
+// One queued unit of work. A partition job covers [start, end) of its source buffer and is
+// cut into chunks on a grid aligned to 16 bytes of the source; its children are written
+// to the other buffer. `dir` follows the reference's `direction`: 1 reads d, 0 reads dn.
+struct alignas(16) Job {
+  unsigned long long start, end;
+  unsigned long long sstart, send;  // reservation cursors: less-than grows up, greater-than down
+  unsigned long long pivot;         // comparison key of the pivot
+  long long grid;                   // element index of the chunk grid origin (may be < start)
+  uint32_t kind, dir, nchunks, cursor;
+  uint32_t remaining, depth, ready, pad;
+};
+static_assert(sizeof(Job) == 80, "job record layout");
+
+// Per-sort device state. Reset by the host (memset) before the seed kernel.
+struct Queue {
+  unsigned long long total;  // keys in this sort
+  unsigned long long done;   // keys in their final place
+  uint32_t head, tail;       // first job with chunks left to take; jobs allocated
+  uint32_t error, pad0;
+  unsigned long long error_info;
+  unsigned long long part_keys, local_keys, tiny_keys, fill_keys, chunks;
+  uint32_t part_jobs, local_jobs, fill_jobs, max_depth;
+};
+
+template <class T>
+struct KeyOps;
+template <>
+struct KeyOps<uint32_t> {
+  using B = uint32_t;
+  static __device__ __forceinline__ B key(B v) { return v; }
+  static __device__ __forceinline__ B raw(B k) { return k; }
+  static constexpr bool kIdentity = true;
+};
+template <>
+struct KeyOps<float> {
+  using B = uint32_t;
+  static __device__ __forceinline__ B key(B u) { return u ^ ((uint32_t)((int32_t)u >> 31) | 0x80000000u); }
+  static __device__ __forceinline__ B raw(B k) { return k ^ (~(uint32_t)((int32_t)k >> 31) | 0x80000000u); }
+  static constexpr bool kIdentity = false;
+};
+template <>
+struct KeyOps<double> {
+  using B = uint64_t;
+  static __device__ __forceinline__ B key(B u) {
+    return u ^ ((uint64_t)((int64_t)u >> 63) | 0x8000000000000000ull);
+  }
+  static __device__ __forceinline__ B raw(B k) {
+    return k ^ (~(uint64_t)((int64_t)k >> 63) | 0x8000000000000000ull);
+  }
+  static constexpr bool kIdentity = false;
+};
+
+template <class T>
+struct SortArgs {
+  typename KeyOps<T>::B* d;
+  typename KeyOps<T>::B* dn;
+  Job* jobs;
+  Queue* q;
+  uint32_t capacity;
+  uint32_t epoch;
+  unsigned long long timeout_ns;
+};
+
+// Kernel configuration. TILE keys fit one local (on-chip) sort; CHUNK keys are one staged
+// partition chunk; TINY = 32*R keys are sorted in registers by one warp.
+template <class T_, int NCW_, int TILE_, int CHUNK_, int STAGES_, int R_, int WARP_MAX_>
+struct Cfg {
+  using T = T_;
+  using Ops = KeyOps<T>;
+  using B = typename Ops::B;
+  static constexpr int NCW = NCW_;
+  static constexpr int NC = NCW * 32;
+  static constexpr int NT = NC + 64;
+  static constexpr int TILE = TILE_;
+  static constexpr int CHUNK = CHUNK_;
+  static constexpr int STAGES = STAGES_;
+  static constexpr int R = R_;
+  static constexpr int TINY = 32 * R;
+  static constexpr int WARP_MAX = WARP_MAX_;
+  static constexpr int KPT = CHUNK / NC;
+  static constexpr int E16 = 16 / (int)sizeof(B);
+  static constexpr int STAGE_ELEMS = CHUNK + 2 * E16;
+  static constexpr int TILE_ELEMS = TILE + 2 * E16;
+  static constexpr int FILL_INLINE = 16384;  // pivot runs up to this many keys are written by the completer
+  static constexpr int FILL_CHUNK = 32768;   // longer runs become queued fill jobs of this grain
+  static constexpr int CQ = 64;              // completer queue slots
+  static constexpr int WLIST = 512;          // segments handed from the CTA phase to the warp phase
+  static constexpr int CSTACK = 48;          // CTA-phase stack (smaller child first: depth <= log2 TILE + 1)
+  static constexpr int WSTACK = 24;          // per-warp stack (same bound for WARP_MAX)
+  static_assert(CHUNK % NC == 0, "chunk must be a multiple of the consumer threads");
+  static_assert((CHUNK * sizeof(B)) % 16 == 0, "chunk must be a multiple of 16 bytes");
+  static_assert(TILE > TINY, "tile must exceed the register sort");
+};
+
+struct Seg {
+  uint32_t s, e, buf;
+};
+
+struct Desc {
+  unsigned long long gbeg;  // first element (global index) of the staged range
+  unsigned long long pivot;
+  uint32_t len, off, job, kind, dir, pad;
+};
+
+template <class C>
+struct alignas(128) Smem {
+  typename C::B stage[C::STAGES][C::STAGE_ELEMS];
+  typename C::B tileA[C::TILE_ELEMS];
+  typename C::B tileB[C::TILE_ELEMS];
+  uint64_t full[C::STAGES], empty[C::STAGES], lfull, lempty;
+  Desc desc[C::STAGES];
+  uint32_t wlt[3][C::NCW], wgt[3][C::NCW];  // per-warp totals: count (k), scatter (k-1), free (k-2)
+  unsigned long long blt[3], bgt[3];
+  uint32_t cq[C::CQ];
+  uint32_t cq_head, cq_tail, term, cons_ok, lok;
+  int csp, wl_n, wl_next;
+  unsigned long long pivot_bc;
+  Seg cstack[C::CSTACK];
+  Seg wlist[C::WLIST];
+  Seg wstack[C::NCW][C::WSTACK];
+};
+
+// ---------------------------------------------------------------------------
+// Error reporting and bounded waits.
+
+__device__ __forceinline__ void set_error(Queue* q, uint32_t code, unsigned long long info) {
+  if (atomicCAS(&q->error, 0u, code) == 0u) q->error_info = info;
+}
+
+__device__ __forceinline__ unsigned long long progress_word(Queue* q) {
+  return ld_relaxed(&q->done) + ((unsigned long long)ld_relaxed(&q->tail) << 40) +
+         ((unsigned long long)ld_relaxed(&q->head) << 20);
+}
+
+// A wait that gives up (and records a timeout) only when the whole sort has made no
+// progress for `timeout_ns`, or when another CTA has already recorded an error.
+struct Waiter {
+  unsigned long long t0, last;
+  uint32_t spins;
+  __device__ __forceinline__ explicit Waiter(Queue* q) : t0(global_timer_ns()), last(progress_word(q)), spins(0) {}
+  __device__ __forceinline__ bool step(Queue* q, unsigned long long timeout_ns, uint32_t where, bool sleep) {
+    ++spins;
+    if ((spins & 31u) == 0u) {
+      if (ld_relaxed(&q->error)) return false;
+      unsigned long long p = progress_word(q), now = global_timer_ns();
+      if (p != last) {
+        last = p;
+        t0 = now;
+      } else if (now - t0 > timeout_ns) {
+        set_error(q, ST_TIMEOUT, where);
+        return false;
+      }
+    }
+    if (sleep) __nanosleep(spins < 64 ? 64 : 512);
+    return true;
+  }
+};
+
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, Queue* q, unsigned long long tmo,
+                                          uint32_t where) {
+  if (mbar_test(bar, parity)) return true;
+  Waiter w(q);
+  while (!mbar_test(bar, parity)) {
+    if (!w.step(q, tmo, where, false)) return false;
+  }
+  return true;
+}
+
+// ---------------------------------------------------------------------------
+// Warp-level bitonic sort of 32*R keys held R per lane; network element e = lane*R + r.
+// (Replaces the reference's work-group bitonic network, QuicksortKernels.cl:40-68.)
+template <int R, class K>
+__device__ __forceinline__ void warp_bitonic(K (&v)[R]) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int k = 2; k <= 32 * R; k <<= 1) {
+#pragma unroll
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      if (j < R) {
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+          const int pr = r ^ j;
+          if (pr > r) {
+            const bool asc = (((lane * R + r) & k) == 0);
+            K a = v[r], b = v[pr];
+            K lo = a < b ? a : b, hi = a < b ? b : a;
+            v[r] = asc ? lo : hi;
+            v[pr] = asc ? hi : lo;
+          }
+        }
+      } else {
+        const int lj = j / R;
+        const bool lower = (lane & lj) == 0;
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+          const bool asc = (((lane * R + r) & k) == 0);
+          K b = __shfl_xor_sync(0xffffffffu, v[r], lj);
+          K a = v[r];
+          K lo = a < b ? a : b, hi = a < b ? b : a;
+          v[r] = (lower == asc) ? lo : hi;
+        }
+      }
+    }
+  }
+}
+
+template <class K>
+__device__ __forceinline__ K kmax() {
+  return ~K(0);
+}
+
+// ---------------------------------------------------------------------------
+// Queue operations.
+
+template <class C>
+__device__ bool push_job(const SortArgs<typename C::T>& a, uint32_t kind, uint32_t dir,
+                         unsigned long long start, unsigned long long end, unsigned long long pivot,
+                         uint32_t depth) {
+  using B = typename C::B;
+  const uint32_t slot = atomicAdd(&a.q->tail, 1u);
+  if (slot >= a.capacity) {
+    set_error(a.q, ST_CAPACITY, slot);
+    return false;
+  }
+  Job* j = a.jobs + slot;
+  long long grid = (long long)start;
+  uint32_t nch = 1;
+  if (kind == JOB_PART) {
+    const B* src = dir ? a.d : a.dn;
+    grid -= (long long)((reinterpret_cast<uintptr_t>(src + start) & 15u) / sizeof(B));
+    nch = (uint32_t)(((long long)end - grid + C::CHUNK - 1) / C::CHUNK);
+  } else if (kind == JOB_FILL) {
+    grid -= (long long)((reinterpret_cast<uintptr_t>(a.d + start) & 15u) / sizeof(B));
+    nch = (uint32_t)(((long long)end - grid + C::FILL_CHUNK - 1) / C::FILL_CHUNK);
+  }
+  j->start = start;
+  j->end = end;
+  j->sstart = start;
+  j->send = end;
+  j->pivot = pivot;
+  j->grid = grid;
+  j->kind = kind;
+  j->dir = dir;
+  j->nchunks = nch;
+  j->cursor = 0;
+  j->remaining = nch;
+  j->depth = depth;
+  __threadfence();
+  st_release(&j->ready, a.epoch);
+  return true;
+}
+
+// Median of 32*RS evenly spaced samples of src[a, a+m) (global memory, L2 reads).
+template <class C, int RS>
+__device__ typename C::B sample_pivot_global(const typename C::B* src, unsigned long long a,
+                                             unsigned long long m) {
+  using B = typename C::B;
+  const int lane = threadIdx.x & 31;
+  B v[RS];
+#pragma unroll
+  for (int r = 0; r < RS; ++r) {
+    const unsigned long long idx = (unsigned long long)(lane * RS + r);
+    v[r] = C::Ops::key(__ldcg(src + a + (idx * m) / (32ull * RS)));
+  }
+  warp_bitonic<RS>(v);
+  return __shfl_sync(0xffffffffu, v[0], 16);
+}
+
+// One warp sorts src[a, a+m) (m <= TINY) into d[a, a+m).
+template <class C>
+__device__ void warp_sort_global(const typename C::B* src, typename C::B* d, unsigned long long a, uint32_t m) {
+  using B = typename C::B;
+  const int lane = threadIdx.x & 31;
+  B v[C::R];
+#pragma unroll
+  for (int r = 0; r < C::R; ++r) {
+    const uint32_t e = lane * C::R + r;
+    v[r] = e < m ? C::Ops::key(__ldcg(src + a + e)) : kmax<B>();
+  }
+  warp_bitonic<C::R>(v);
+#pragma unroll
+  for (int r = 0; r < C::R; ++r) {
+    const uint32_t e = lane * C::R + r;
+    if (e < m) d[a + e] = C::Ops::raw(v[r]);
+  }
+}
+
+// Decide what to do with a range whose keys sit in `src` (dir says which buffer that is).
+// Called by a whole warp. Returns the number of keys placed in their final position.
+template <class C>
+__device__ unsigned long long dispatch_range(const SortArgs<typename C::T>& a, uint32_t dir,
+                                             unsigned long long s, unsigned long long e, uint32_t depth,
+                                             unsigned long long& tiny_keys) {
+  using B = typename C::B;
+  const int lane = threadIdx.x & 31;
+  const unsigned long long m = e - s;
+  B* src = dir ? a.d : a.dn;
+  if (m == 0) return 0;
+  if (m == 1) {
+    if (!dir && lane == 0) a.d[s] = __ldcg(src + s);
+    return 1;
+  }
+  if (m <= (unsigned long long)C::TINY) {
+    warp_sort_global<C>(src, a.d, s, (uint32_t)m);
+    tiny_keys += m;
+    return m;
+  }
+  if (m <= (unsigned long long)C::TILE) {
+    if (lane == 0) push_job<C>(a, JOB_LOCAL, dir, s, e, 0, depth);
+    return 0;
+  }
+  const B pv = sample_pivot_global<C, 4>(src, s, m);
+  if (lane == 0) push_job<C>(a, JOB_PART, dir, s, e, (unsigned long long)pv, depth);
+  return 0;
+}
+
+// ---------------------------------------------------------------------------
+// Seed kernel: one warp per segment turns the segment table into root jobs.
+
+template <class C>
+__global__ void __launch_bounds__(256) seed_kernel(SortArgs<typename C::T> a, const unsigned long long* offsets,
+                                                   uint32_t nseg, unsigned long long n) {
+  const uint32_t seg = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (seg >= nseg) return;
+  const unsigned long long s = offsets ? offsets[seg] : 0ull, e = offsets ? offsets[seg + 1] : n;
+  if (s > e || e > n) {  // malformed segment table
+    if (lane == 0) set_error(a.q, ST_INVALID, seg);
+    return;
+  }
+  if (e == s) return;
+  if (lane == 0) atomicAdd(&a.q->total, e - s);
+  unsigned long long tiny = 0;
+  const unsigned long long placed = dispatch_range<C>(a, 1u, s, e, 0u, tiny);
+  if (lane == 0) {
+    if (placed) atomicAdd(&a.q->done, placed);
+    if (tiny) atomicAdd(&a.q->tiny_keys, tiny);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Persistent sort kernel.
+
+template <class C>
+struct Persistent {
+  using T = typename C::T;
+  using B = typename C::B;
+  using Ops = typename C::Ops;
+
+  static __device__ __forceinline__ void cbar() { named_bar_sync(1, C::NC); }
+
+  // ---- producer ---------------------------------------------------------
+  // Take one chunk of the oldest job that still has chunks. Returns ITEM_NONE when the queue
+  // is momentarily empty, ITEM_TERM when every key is placed or the sort has failed.
+  static __device__ uint32_t grab(const SortArgs<T>& a, uint32_t& slot, uint32_t& chunk) {
+    for (;;) {
+      if (ld_relaxed(&a.q->error)) return ITEM_TERM;
+      const uint32_t h = ld_relaxed(&a.q->head);
+      const uint32_t t = ld_relaxed(&a.q->tail);
+      if (h < t) {
+        if (h >= a.capacity) return ITEM_TERM;
+        Job* j = a.jobs + h;
+        if (ld_acquire(&j->ready) != a.epoch) return ITEM_NONE;  // allocated, not yet published
+        const uint32_t nch = __ldcg(&j->nchunks);
+        const uint32_t c = atomicAdd(&j->cursor, 1u);
+        if (c < nch) {
+          slot = h;
+          chunk = c;
+          return __ldcg(&j->kind);
+        }
+        atomicCAS(&a.q->head, h, h + 1);
+        continue;
+      }
+      if (ld_relaxed(&a.q->done) >= ld_relaxed(&a.q->total)) return ITEM_TERM;
+      return ITEM_NONE;
+    }
+  }
+
+  // Stage src[cs, ce) into shared memory at `dst`, rounded out to whole 16-byte granules of
+  // global memory (a granule never straddles a page, so the rounding cannot fault; the extra
+  // bytes are never read). Returns the element offset of src[cs] inside `dst`.
+  static __device__ __forceinline__ uint32_t stage_range(const B* src, unsigned long long cs,
+                                                         unsigned long long ce, B* dst, uint64_t* bar) {
+    const uintptr_t lo = reinterpret_cast<uintptr_t>(src + cs);
+    const uintptr_t ga = lo & ~uintptr_t(15);
+    const uintptr_t gb = (reinterpret_cast<uintptr_t>(src + ce) + 15) & ~uintptr_t(15);
+    const uint32_t bytes = (uint32_t)(gb - ga);
+    fence_proxy_async_smem();
+    mbar_arrive_expect_tx(bar, bytes);
+    bulk_load(dst, reinterpret_cast<const void*>(ga), bytes, bar);
+    return (uint32_t)((lo - ga) / sizeof(B));
+  }
+
+  static __device__ void producer(const SortArgs<T>& a, Smem<C>& sm) {
+    const int lane = threadIdx.x & 31;
+    uint32_t k = 0, nloc = 0;
+    bool need_flush = false;  // partition chunks were handed out since the last drain
+    uint32_t failed = 0;
+    Waiter idle(a.q);
+    bool idling = false;
+    for (;;) {
+      uint32_t kind = ITEM_NONE, slot = 0, chunk = 0;
+      if (lane == 0) {
+        kind = grab(a, slot, chunk);
+        if (kind == ITEM_NONE) {
+          if (need_flush) {
+            kind = ITEM_FLUSH;  // let the consumers finish what they hold before idling
+          } else {
+            if (!idling) {
+              idle = Waiter(a.q);
+              idling = true;
+            }
+            if (!idle.step(a.q, a.timeout_ns, 1, true)) kind = ITEM_TERM;
+          }
+        } else {
+          idling = false;
+        }
+      }
+      kind = __shfl_sync(0xffffffffu, kind, 0);
+      if (kind == ITEM_NONE) continue;
+      const uint32_t s = k % C::STAGES;
+      if (lane == 0) {
+        if (!mbar_wait(&sm.empty[s], ((k / C::STAGES) & 1u) ^ 1u, a.q, a.timeout_ns, 2)) {
+          failed = 1;
+        } else if (kind == ITEM_TERM || kind == ITEM_FLUSH) {
+          sm.desc[s].kind = kind;
+          mbar_arrive(&sm.full[s]);
+          need_flush = false;
+        } else {
+          const Job* j = a.jobs + slot;
+          const unsigned long long js = __ldcg(&j->start), je = __ldcg(&j->end);
+          const uint32_t dir = __ldcg(&j->dir);
+          Desc& dd = sm.desc[s];
+          dd.kind = kind;
+          dd.job = slot;
+          dd.dir = dir;
+          dd.pivot = __ldcg(&j->pivot);
+          const B* src = dir ? a.d : a.dn;
+          if (kind == ITEM_PART || kind == ITEM_FILL) {
+            const long long grain = kind == ITEM_PART ? C::CHUNK : C::FILL_CHUNK;
+            const long long g0 = __ldcg(&j->grid) + (long long)chunk * grain;
+            const unsigned long long cs = (long long)js > g0 ? js : (unsigned long long)g0;
+            const unsigned long long ce0 = (unsigned long long)(g0 + grain);
+            const unsigned long long ce = ce0 < je ? ce0 : je;
+            dd.gbeg = cs;
+            dd.len = (uint32_t)(ce - cs);
+            if (kind == ITEM_PART) {
+              dd.off = stage_range(src, cs, ce, sm.stage[s], &sm.full[s]);
+              need_flush = true;
+            } else {
+              dd.off = 0;
+              mbar_arrive(&sm.full[s]);
+              need_flush = false;
+            }
+          } else {  // ITEM_LOCAL: the tile region is single-buffered
+            if (!mbar_wait(&sm.lempty, (nloc & 1u) ^ 1u, a.q, a.timeout_ns, 3)) {
+              failed = 1;
+            } else {
+              dd.gbeg = js;
+              dd.len = (uint32_t)(je - js);
+              dd.off = stage_range(src, js, je, sm.tileA, &sm.lfull);
+              mbar_arrive(&sm.full[s]);
+              ++nloc;
+              need_flush = false;
+            }
+          }
+        }
+      }
+      failed = __shfl_sync(0xffffffffu, failed, 0);
+      if (failed) break;
+      ++k;
+      if (kind == ITEM_TERM) break;
+    }
+    if (failed && lane == 0) {
+      // Leave no bulk copy in flight into this CTA's shared memory: each stage's most recent
+      // load completes on its full barrier, the most recent tile load on lfull.
+      for (uint32_t i = 0; i < (uint32_t)C::STAGES && i < k; ++i) {
+        const uint32_t kk = k - 1 - i;
+        mbar_wait(&sm.full[kk % C::STAGES], (kk / C::STAGES) & 1u, a.q, 200000000ull, 9);
+      }
+      if (nloc) mbar_wait(&sm.lfull, (nloc - 1) & 1u, a.q, 200000000ull, 9);
+      sts_release(&sm.term, 2u);
+    }
+  }
+
+  // ---- completer --------------------------------------------------------
+  static __device__ void complete_job(const SortArgs<T>& a, uint32_t slot, unsigned long long& st_tiny,
+                                      unsigned long long& st_fill, uint32_t& st_depth) {
+    const int lane = threadIdx.x & 31;
+    const Job* j = a.jobs + slot;
+    const unsigned long long js = __ldcg(&j->start), je = __ldcg(&j->end);
+    const unsigned long long ss = __ldcg(&j->sstart), se = __ldcg(&j->send);
+    const B pv = (B)__ldcg(&j->pivot);
+    const uint32_t dir = __ldcg(&j->dir), depth = __ldcg(&j->depth);
+    unsigned long long placed = 0;
+    // Pivot run [ss, se) -> d (the reference's last block writes it serially,
+    // QuicksortKernels.cl:214-216; here a warp writes short runs and long runs become
+    // fill jobs that every CTA shares).
+    const unsigned long long plen = se - ss;
+    if (plen) {
+      if (plen <= (unsigned long long)C::FILL_INLINE) {
+        const B raw = Ops::raw(pv);
+        for (unsigned long long i = ss + lane; i < se; i += 32) a.d[i] = raw;
+        placed += plen;
+        st_fill += plen;
+      } else if (lane == 0) {
+        push_job<C>(a, JOB_FILL, 0u, ss, se, (unsigned long long)pv, depth);
+      }
+    }
+    // Children live in this job's destination buffer; they are read the other way next.
+    const uint32_t cdir = dir ^ 1u;
+    placed += dispatch_range<C>(a, cdir, js, ss, depth + 1, st_tiny);
+    placed += dispatch_range<C>(a, cdir, se, je, depth + 1, st_tiny);
+    if (lane == 0 && placed) atomicAdd(&a.q->done, placed);
+    if (depth + 1 > st_depth) st_depth = depth + 1;
+  }
+
+  static __device__ void completer(const SortArgs<T>& a, Smem<C>& sm) {
+    const int lane = threadIdx.x & 31;
+    unsigned long long st_tiny = 0, st_fill = 0;
+    uint32_t st_depth = 0, st_jobs = 0;
+    uint32_t head = 0;
+    Waiter w(a.q);
+    bool idling = false;
+    for (;;) {
+      uint32_t slot = 0, state = 0;  // 0 none, 1 item, 2 exit
+      if (lane == 0) {
+        const uint32_t t = lds_acquire(&sm.cq_tail);
+        if (t != head) {
+          slot = sm.cq[head % C::CQ];
+          ++head;
+          sts_release(&sm.cq_head, head);
+          state = 1;
+          idling = false;
+        } else if (lds_acquire(&sm.term)) {
+          state = 2;
+        } else {
+          if (!idling) {
+            w = Waiter(a.q);
+            idling = true;
+          }
+          if (!w.step(a.q, a.timeout_ns, 4, true)) state = 2;  // the sort failed; nothing left to finish
+        }
+      }
+      state = __shfl_sync(0xffffffffu, state, 0);
+      if (state == 2) break;
+      if (state == 0) continue;
+      slot = __shfl_sync(0xffffffffu, slot, 0);
+      uint32_t old = 0;
+      if (lane == 0) {
+        __threadfence();
+        old = atomicSub(&a.jobs[slot].remaining, 1u);
+        __threadfence();
+      }
+      old = __shfl_sync(0xffffffffu, old, 0);
+      if (old == 1u) {
+        complete_job(a, slot, st_tiny, st_fill, st_depth);
+        ++st_jobs;
+      }
+    }
+    if (lane == 0) {
+      if (st_tiny) atomicAdd(&a.q->tiny_keys, st_tiny);
+      if (st_fill) atomicAdd(&a.q->fill_keys, st_fill);
+      if (st_jobs) atomicAdd(&a.q->part_jobs, st_jobs);
+      atomicMax(&a.q->max_depth, st_depth);
+    }
+  }
+
+  // ---- consumers: partition chunks --------------------------------------
+  // Post a finished chunk of job `slot` to this CTA's completer.
+  static __device__ void post_chunk(const SortArgs<T>& a, Smem<C>& sm, uint32_t slot) {
+    const uint32_t t = sm.cq_tail;
+    if (t - lds_acquire(&sm.cq_head) >= (uint32_t)C::CQ) {
+      Waiter w(a.q);
+      while (t - lds_acquire(&sm.cq_head) >= (uint32_t)C::CQ) {
+        if (!w.step(a.q, a.timeout_ns, 5, false)) return;
+      }
+    }
+    sm.cq[t % C::CQ] = slot;
+    sts_release(&sm.cq_tail, t + 1);
+  }
+
+  // Scatter one counted chunk whose keys are in registers: keys below the pivot go to
+  // [lb + warp prefix ...), keys above to [gb + warp prefix ...). Equal keys are dropped; the
+  // completer writes the pivot run. (gqsort_kernel pass 2, QuicksortKernels.cl:190-203.)
+  static __device__ __forceinline__ void scatter_chunk(const B (&keys)[C::KPT], uint32_t len, B p, B* dst,
+                                                       unsigned long long lb, unsigned long long gb,
+                                                       const uint32_t* wlt, const uint32_t* wgt) {
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    uint32_t vl = lane < C::NCW ? wlt[lane] : 0u, vg = lane < C::NCW ? wgt[lane] : 0u;
+    uint32_t il = vl, ig = vg;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t tl = __shfl_up_sync(0xffffffffu, il, o), tg = __shfl_up_sync(0xffffffffu, ig, o);
+      if (lane >= o) {
+        il += tl;
+        ig += tg;
+      }
+    }
+    const unsigned long long lpos0 = lb + (unsigned long long)__shfl_sync(0xffffffffu, il - vl, warp);
+    const unsigned long long gpos0 = gb + (unsigned long long)__shfl_sync(0xffffffffu, ig - vg, warp);
+    unsigned long long lpos = lpos0, gpos = gpos0;
+    const uint32_t ltm = lanemask_lt();
+#pragma unroll
+    for (int j = 0; j < C::KPT; ++j) {
+      const uint32_t i = (uint32_t)(j * C::NC + tid);
+      const bool valid = i < len;
+      const B kk = Ops::key(keys[j]);
+      const bool isl = valid && kk < p, isg = valid && kk > p;
+      const uint32_t bl = __ballot_sync(0xffffffffu, isl), bg = __ballot_sync(0xffffffffu, isg);
+      if (isl) dst[lpos + __popc(bl & ltm)] = keys[j];
+      if (isg) dst[gpos + __popc(bg & ltm)] = keys[j];
+      lpos += __popc(bl);
+      gpos += __popc(bg);
+    }
+  }
+
+  // ---- consumers: local (on-chip) sort -----------------------------------
+  static __device__ __forceinline__ B* bufp(Smem<C>& sm, B* A, uint32_t buf) { return buf ? sm.tileB : A; }
+
+  // One warp sorts X[s, s+n) (n <= TINY) into A[s, s+n).
+  static __device__ __forceinline__ void warp_sort_smem(const B* X, B* A, uint32_t s, uint32_t n) {
+    const int lane = threadIdx.x & 31;
+    B v[C::R];
+#pragma unroll
+    for (int r = 0; r < C::R; ++r) {
+      const uint32_t e = r * 32 + lane;  // any input layout is valid; this one is bank-conflict free
+      v[r] = e < n ? X[s + e] : kmax<B>();
+    }
+    __syncwarp();
+    warp_bitonic<C::R>(v);
+#pragma unroll
+    for (int r = 0; r < C::R; ++r) {
+      const uint32_t e = lane * C::R + r;
+      if (e < n) A[s + e] = v[r];
+    }
+    __syncwarp();
+  }
+
+  // Median of 32 evenly spaced samples of X[s, s+n), computed by one warp.
+  static __device__ __forceinline__ B sample32_smem(const B* X, uint32_t s, uint32_t n) {
+    const int lane = threadIdx.x & 31;
+    B v[1];
+    v[0] = X[s + (uint32_t)(((unsigned long long)lane * n) >> 5)];
+    warp_bitonic<1>(v);
+    return __shfl_sync(0xffffffffu, v[0], 16);
+  }
+
+  // Place a child segment: singletons go straight to A, small ones to the warp list,
+  // the rest to the CTA stack. Called by one thread.
+  static __device__ __forceinline__ void push_child(Smem<C>& sm, B* A, uint32_t s, uint32_t e, uint32_t buf,
+                                                    Queue* q) {
+    const uint32_t n = e - s;
+    if (n == 0) return;
+    if (n == 1) {
+      if (buf) A[s] = sm.tileB[s];
+      return;
+    }
+    if (n <= (uint32_t)C::WARP_MAX && sm.wl_n < C::WLIST) {
+      sm.wlist[sm.wl_n++] = Seg{s, e, buf};
+      return;
+    }
+    if (sm.csp < C::CSTACK) {
+      sm.cstack[sm.csp++] = Seg{s, e, buf};
+    } else {
+      set_error(q, ST_INTERNAL, 0xC57ACull);
+    }
+  }
+
+  // Warp phase: quicksort of one segment in shared memory with an explicit stack
+  // (lqsort_kernel's work stack, QuicksortKernels.cl:280-420, run by one warp).
+  static __device__ void warp_quicksort(Smem<C>& sm, B* A, Seg seg, Seg* stk, Queue* q) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t ltm = lanemask_lt();
+    int sp = 0;
+    if (lane == 0) stk[0] = seg;
+    sp = 1;
+    __syncwarp();
+    while (sp > 0) {
+      const Seg g = stk[sp - 1];
+      --sp;
+      __syncwarp();
+      const B* X = bufp(sm, A, g.buf);
+      B* Y = bufp(sm, A, g.buf ^ 1u);
+      const uint32_t n = g.e - g.s;
+      if (n <= (uint32_t)C::TINY) {
+        warp_sort_smem(X, A, g.s, n);
+        continue;
+      }
+      const B p = sample32_smem(X, g.s, n);
+      uint32_t lpos = g.s, gpos = g.e;
+      for (uint32_t base = g.s; base < g.e; base += 32) {
+        const uint32_t i = base + lane;
+        const bool valid = i < g.e;
+        const B kk = valid ? X[i] : B(0);
+        const bool isl = valid && kk < p, isg = valid && kk > p;
+        const uint32_t bl = __ballot_sync(0xffffffffu, isl), bg = __ballot_sync(0xffffffffu, isg);
+        if (isl) Y[lpos + __popc(bl & ltm)] = kk;
+        if (isg) Y[gpos - 1 - __popc(bg & ltm)] = kk;
+        lpos += __popc(bl);
+        gpos -= __popc(bg);
+      }
+      __syncwarp();
+      for (uint32_t i = lpos + lane; i < gpos; i += 32) A[i] = p;
+      // children [g.s, lpos) and [gpos, g.e), both in Y
+      const uint32_t cb = g.buf ^ 1u;
+      const uint32_t nl = lpos - g.s, ng = g.e - gpos;
+      int t = sp;
+      if (lane == 0) {
+        if (nl == 1 && cb) A[g.s] = Y[g.s];
+        if (ng == 1 && cb) A[gpos] = Y[gpos];
+        // larger first so the smaller child is popped next (stack depth <= log2 n + 1)
+        const Seg big = nl >= ng ? Seg{g.s, lpos, cb} : Seg{gpos, g.e, cb};
+        const Seg sml = nl >= ng ? Seg{gpos, g.e, cb} : Seg{g.s, lpos, cb};
+        if (big.e - big.s > 1) {
+          if (t < C::WSTACK) stk[t++] = big;
+          else set_error(q, ST_INTERNAL, 0x57ACull);
+        }
+        if (sml.e - sml.s > 1) {
+          if (t < C::WSTACK) stk[t++] = sml;
+          else set_error(q, ST_INTERNAL, 0x57ACull);
+        }
+      }
+      sp = __shfl_sync(0xffffffffu, t, 0);
+      __syncwarp();
+    }
+  }
+
+  // CTA-wide local sort of A[0, m) (keys already mapped to comparison keys). On return A
+  // holds the sorted keys. (lqsort_kernel, QuicksortKernels.cl:267-421.)
+  static __device__ void local_sort(const SortArgs<T>& a, Smem<C>& sm, B* A, uint32_t m) {
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const uint32_t ltm = lanemask_lt();
+    if (tid == 0) {
+      sm.csp = 0;
+      sm.wl_n = 0;
+      sm.wl_next = 0;
+      if (m > (uint32_t)C::WARP_MAX) {
+        sm.cstack[sm.csp++] = Seg{0, m, 0};
+      } else {
+        sm.wlist[sm.wl_n++] = Seg{0, m, 0};
+      }
+    }
+    cbar();
+    for (;;) {
+      const int sp = sm.csp;
+      if (sp == 0) break;
+      const Seg g = sm.cstack[sp - 1];
+      cbar();
+      if (tid == 0) sm.csp = sp - 1;
+      const B* X = bufp(sm, A, g.buf);
+      B* Y = bufp(sm, A, g.buf ^ 1u);
+      const uint32_t n = g.e - g.s;
+      if (n <= (uint32_t)C::TINY) {
+        if (warp == 0) warp_sort_smem(X, A, g.s, n);
+        cbar();
+        continue;
+      }
+      if (warp == 0) {
+        const B pv = sample32_smem(X, g.s, n);
+        if (lane == 0) sm.pivot_bc = (unsigned long long)pv;
+      }
+      cbar();
+      const B p = (B)sm.pivot_bc;
+      uint32_t cl = 0, cg = 0;
+      for (uint32_t i = g.s + tid; i < g.e; i += C::NC) {
+        const B kk = X[i];
+        cl += kk < p;
+        cg += kk > p;
+      }
+      cl = __reduce_add_sync(0xffffffffu, cl);
+      cg = __reduce_add_sync(0xffffffffu, cg);
+      if (lane == 0) {
+        sm.wlt[0][warp] = cl;
+        sm.wgt[0][warp] = cg;
+      }
+      cbar();
+      uint32_t vl = lane < C::NCW ? sm.wlt[0][lane] : 0u, vg = lane < C::NCW ? sm.wgt[0][lane] : 0u;
+      uint32_t il = vl, ig = vg;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t tl = __shfl_up_sync(0xffffffffu, il, o), tg = __shfl_up_sync(0xffffffffu, ig, o);
+        if (lane >= o) {
+          il += tl;
+          ig += tg;
+        }
+      }
+      const uint32_t L = __shfl_sync(0xffffffffu, il, 31), G = __shfl_sync(0xffffffffu, ig, 31);
+      uint32_t lpos = g.s + __shfl_sync(0xffffffffu, il - vl, warp);
+      uint32_t gpos = g.e - G + __shfl_sync(0xffffffffu, ig - vg, warp);
+      // same strided order as the count pass, so each warp's ranks stay within its range
+      for (uint32_t base = g.s; base < g.e; base += C::NC) {
+        const uint32_t i = base + tid;
+        const bool valid = i < g.e;
+        const B kk = valid ? X[i] : B(0);
+        const bool isl = valid && kk < p, isg = valid && kk > p;
+        const uint32_t bl = __ballot_sync(0xffffffffu, isl), bg = __ballot_sync(0xffffffffu, isg);
+        if (isl) Y[lpos + __popc(bl & ltm)] = kk;
+        if (isg) Y[gpos + __popc(bg & ltm)] = kk;
+        lpos += __popc(bl);
+        gpos += __popc(bg);
+      }
+      cbar();
+      for (uint32_t i = g.s + L + tid; i < g.e - G; i += C::NC) A[i] = p;
+      if (tid == 0) {
+        const uint32_t cb = g.buf ^ 1u;
+        const uint32_t ls = g.s, le = g.s + L, gs = g.e - G, ge = g.e;
+        if (L >= G) {
+          push_child(sm, A, ls, le, cb, a.q);
+          push_child(sm, A, gs, ge, cb, a.q);
+        } else {
+          push_child(sm, A, gs, ge, cb, a.q);
+          push_child(sm, A, ls, le, cb, a.q);
+        }
+      }
+      cbar();
+    }
+    // warp phase
+    const int nwl = sm.wl_n;
+    for (;;) {
+      int idx = 0;
+      if (lane == 0) idx = atomicAdd(&sm.wl_next, 1);
+      idx = __shfl_sync(0xffffffffu, idx, 0);
+      if (idx >= nwl) break;
+      warp_quicksort(sm, A, sm.wlist[idx], sm.wstack[warp], a.q);
+    }
+    cbar();
+  }
+
+  // Leader-only bounded wait for ring slot k; every consumer reads the verdict after the
+  // next named barrier, so all consumer threads always take the same path.
+  static __device__ __forceinline__ void leader_wait_slot(const SortArgs<T>& a, Smem<C>& sm, uint32_t k) {
+    sm.cons_ok = mbar_wait(&sm.full[k % C::STAGES], (k / C::STAGES) & 1u, a.q, a.timeout_ns, 6) ? 1u : 0u;
+  }
+
+  static __device__ void consumers(const SortArgs<T>& a, Smem<C>& sm) {
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    uint32_t k = 0, nloc = 0, npart = 0;
+    // pend: counted, offsets requested, scattered next iteration; scat: scattered last
+    // iteration, posted to the completer at the next barrier.
+    bool have_pend = false, have_scat = false;
+    B pend[C::KPT];
+    uint32_t pend_len = 0, pend_job = 0, pend_par = 0, scat_job = 0;
+    B pend_p = 0;
+    B* pend_dst = nullptr;
+    unsigned long long pend_lb = 0, pend_gb = 0;  // leader only
+    unsigned long long st_part = 0, st_local = 0, st_chunks = 0;
+    uint32_t st_local_jobs = 0, st_fill_jobs = 0;
+
+    if (tid == 0) leader_wait_slot(a, sm, 0);
+    cbar();
+    for (;;) {
+      if (!sm.cons_ok) break;
+      const uint32_t s = k % C::STAGES;
+      (void)mbar_test(&sm.full[s], (k / C::STAGES) & 1u);  // completed; gives this thread acquire order
+      const Desc dd = sm.desc[s];
+      if (dd.kind == ITEM_PART) {
+        const B* stg = sm.stage[s] + dd.off;
+        const B p = (B)dd.pivot;
+        B cur[C::KPT];
+        uint32_t cl = 0, cg = 0;
+#pragma unroll
+        for (int j = 0; j < C::KPT; ++j) {
+          const uint32_t i = (uint32_t)(j * C::NC + tid);
+          cur[j] = i < dd.len ? stg[i] : B(0);
+          const B kk = Ops::key(cur[j]);
+          cl += (i < dd.len) && kk < p;
+          cg += (i < dd.len) && kk > p;
+        }
+        const uint32_t par = npart % 3u;
+        cl = __reduce_add_sync(0xffffffffu, cl);
+        cg = __reduce_add_sync(0xffffffffu, cg);
+        if (lane == 0) {
+          sm.wlt[par][warp] = cl;
+          sm.wgt[par][warp] = cg;
+        }
+        cbar();  // #1: stage s read into registers; the previous scatter is complete
+        unsigned long long new_lb = 0, new_gb = 0;
+        if (tid == 0) {
+          mbar_arrive(&sm.empty[s]);
+          if (have_scat) post_chunk(a, sm, scat_job);
+          if (have_pend) {
+            sm.blt[pend_par] = pend_lb;
+            sm.bgt[pend_par] = pend_gb;
+          }
+          uint32_t ls = 0, gs = 0;
+#pragma unroll
+          for (int w = 0; w < C::NCW; ++w) {
+            ls += sm.wlt[par][w];
+            gs += sm.wgt[par][w];
+          }
+          // Reserve this chunk's output ranges in the parent (QuicksortKernels.cl:183-186).
+          // The results are used one iteration later, hiding the atomic round trip.
+          Job* j = a.jobs + dd.job;
+          new_lb = atomicAdd(&j->sstart, (unsigned long long)ls);
+          new_gb = atomicAdd(&j->send, (unsigned long long)(-(long long)gs)) - gs;
+          leader_wait_slot(a, sm, k + 1);
+        }
+        cbar();  // #2: bases of the pending chunk published; next slot verdict published
+        have_scat = false;
+        if (have_pend) {
+          scatter_chunk(pend, pend_len, pend_p, pend_dst, sm.blt[pend_par], sm.bgt[pend_par], sm.wlt[pend_par],
+                        sm.wgt[pend_par]);
+          have_scat = true;
+          scat_job = pend_job;
+        }
+#pragma unroll
+        for (int j = 0; j < C::KPT; ++j) pend[j] = cur[j];
+        pend_len = dd.len;
+        pend_job = dd.job;
+        pend_par = par;
+        pend_p = p;
+        pend_dst = dd.dir ? a.dn : a.d;
+        pend_lb = new_lb;
+        pend_gb = new_gb;
+        have_pend = true;
+        st_part += dd.len;
+        ++st_chunks;
+        ++npart;
+        ++k;
+        continue;
+      }
+
+      // Any other item first drains the pipeline of partition chunks.
+      if (tid == 0) {
+        if (have_scat) post_chunk(a, sm, scat_job);
+        if (have_pend) {
+          sm.blt[pend_par] = pend_lb;
+          sm.bgt[pend_par] = pend_gb;
+        }
+      }
+      cbar();
+      if (have_pend) {
+        scatter_chunk(pend, pend_len, pend_p, pend_dst, sm.blt[pend_par], sm.bgt[pend_par], sm.wlt[pend_par],
+                      sm.wgt[pend_par]);
+      }
+      cbar();
+      if (tid == 0) {
+        if (have_pend) post_chunk(a, sm, pend_job);
+        mbar_arrive(&sm.empty[s]);  // every thread copied the descriptor before the barriers above
+      }
+      have_pend = false;
+      have_scat = false;
+
+      if (dd.kind == ITEM_TERM) break;
+      if (dd.kind == ITEM_FILL) {
+        // Queued pivot-run fill: write the raw pivot over d[gbeg, gbeg + len).
+        const B raw = Ops::raw((B)dd.pivot);
+        B* out = a.d + dd.gbeg;
+        for (uint32_t i = tid; i < dd.len; i += C::NC) out[i] = raw;
+        ++st_fill_jobs;
+        if (tid == 0) atomicAdd(&a.q->done, (unsigned long long)dd.len);
+      } else if (dd.kind == ITEM_LOCAL) {
+        if (tid == 0) sm.lok = mbar_wait(&sm.lfull, nloc & 1u, a.q, a.timeout_ns, 7) ? 1u : 0u;
+        cbar();
+        if (!sm.lok) break;
+        (void)mbar_test(&sm.lfull, nloc & 1u);
+        B* A = sm.tileA + dd.off;
+        const uint32_t m = dd.len;
+        if (!Ops::kIdentity) {
+          for (uint32_t i = tid; i < m; i += C::NC) A[i] = Ops::key(A[i]);
+          cbar();
+        }
+        local_sort(a, sm, A, m);
+        if (!Ops::kIdentity) {
+          for (uint32_t i = tid; i < m; i += C::NC) A[i] = Ops::raw(A[i]);
+        }
+        // Write the sorted tile to d: one bulk TMA store for the 16-byte-aligned body,
+        // plain stores for the ragged ends (a bulk store must not touch bytes outside).
+        B* out = a.d + dd.gbeg;
+        const uintptr_t olo = reinterpret_cast<uintptr_t>(out);
+        const uintptr_t ohi = reinterpret_cast<uintptr_t>(out + m);
+        const uintptr_t ga = (olo + 15) & ~uintptr_t(15), gb = ohi & ~uintptr_t(15);
+        const uint32_t head = (uint32_t)((ga - olo) / sizeof(B));
+        const bool tma_ok = ga < gb && ((smem_addr(A + head) & 15u) == 0u);
+        if (tma_ok) {
+          fence_proxy_async_smem();
+          cbar();
+          const uint32_t tail0 = (uint32_t)((gb - olo) / sizeof(B));
+          if (tid == 0) {
+            bulk_store(reinterpret_cast<void*>(ga), A + head, (uint32_t)(gb - ga));
+            bulk_commit();
+          }
+          for (uint32_t i = tid; i < head; i += C::NC) out[i] = A[i];
+          for (uint32_t i = tail0 + tid; i < m; i += C::NC) out[i] = A[i];
+          if (tid == 0) bulk_wait_read_all();
+        } else {
+          cbar();
+          for (uint32_t i = tid; i < m; i += C::NC) out[i] = A[i];
+        }
+        cbar();  // every read of the tile is done before the producer may refill it
+        if (tid == 0) {
+          mbar_arrive(&sm.lempty);
+          atomicAdd(&a.q->done, (unsigned long long)m);
+        }
+        st_local += m;
+        ++st_local_jobs;
+        ++nloc;
+      }
+      // ITEM_FLUSH needs nothing beyond the drain above.
+      if (tid == 0) leader_wait_slot(a, sm, k + 1);
+      cbar();
+      ++k;
+    }
+    if (tid == 0) {
+      bulk_wait_all();
+      sts_release(&sm.term, 1u);
+      if (st_part) atomicAdd(&a.q->part_keys, st_part);
+      if (st_local) atomicAdd(&a.q->local_keys, st_local);
+      if (st_chunks) atomicAdd(&a.q->chunks, st_chunks);
+      if (st_local_jobs) atomicAdd(&a.q->local_jobs, st_local_jobs);
+      if (st_fill_jobs) atomicAdd(&a.q->fill_jobs, st_fill_jobs);
+    }
+  }
+};
+
+template <class C>
+__global__ void __launch_bounds__(C::NT, 1) persistent_kernel(SortArgs<typename C::T> a) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  Smem<C>& sm = *reinterpret_cast<Smem<C>*>(smem_raw);
+  const int tid = threadIdx.x;
+  if (tid == 0) {
+    for (int i = 0; i < C::STAGES; ++i) {
+      mbar_init(&sm.full[i], 1);
+      mbar_init(&sm.empty[i], 1);
+    }
+    mbar_init(&sm.lfull, 1);
+    mbar_init(&sm.lempty, 1);
+    sm.cq_head = 0;
+    sm.cq_tail = 0;
+    sm.term = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  const int warp = tid >> 5;
+  if (warp < C::NCW) {
+    Persistent<C>::consumers(a, sm);
+  } else if (warp == C::NCW) {
+    Persistent<C>::producer(a, sm);
+  } else {
+    Persistent<C>::completer(a, sm);
+  }
+}
+
+}  // namespace gqs

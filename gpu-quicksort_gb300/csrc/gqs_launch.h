@@ -1,0 +1,63 @@
+// Internal launch interface between the C ABI (gqs_capi.cu) and the per-key-type
+// translation units that instantiate the kernels (gqs_sort_{u32,f32,f64}.cu).
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace gqs {
+
+struct Job;
+struct Queue;
+
+enum DType : int { DT_U32 = 0, DT_F32 = 1, DT_F64 = 2 };
+
+struct VariantInfo {
+  int ncw;         // consumer warps per CTA
+  int threads;     // threads per CTA (consumers + producer + completer)
+  int tile;        // keys sorted on chip by one local job (the gqsort -> lqsort switch)
+  int chunk;       // keys per staged partition chunk
+  int kpt;         // keys per consumer thread per chunk
+  int stages;      // chunks in flight per CTA
+  int tiny;        // keys sorted in registers by one warp
+  size_t smem;     // dynamic shared memory per CTA
+  const char* name;
+};
+
+struct LaunchParams {
+  void* d;
+  void* dn;
+  Job* jobs;
+  Queue* q;
+  uint32_t capacity;
+  uint32_t epoch;
+  unsigned long long timeout_ns;
+  const unsigned long long* offsets;  // nseg + 1 device offsets, or null for one segment [0, n)
+  unsigned long long n;               // keys when offsets is null
+  uint32_t nseg;
+  int variant;
+  int grid;
+  cudaStream_t stream;
+  cudaEvent_t ev_begin;  // optional: recorded around the persistent kernel
+  cudaEvent_t ev_end;
+};
+
+// Per key type (defined in gqs_sort_<type>.cu).
+#define GQS_DECLARE_TYPE(S)                         \
+  int variant_count_##S();                          \
+  VariantInfo variant_info_##S(int v);              \
+  int variant_prepare_##S(int v);                   \
+  cudaError_t launch_##S(const LaunchParams& p);
+GQS_DECLARE_TYPE(u32)
+GQS_DECLARE_TYPE(f32)
+GQS_DECLARE_TYPE(f64)
+#undef GQS_DECLARE_TYPE
+
+// Dispatch by key type (defined in gqs_capi.cu).
+int variant_count(int dtype);
+VariantInfo variant_info(int dtype, int v);
+// Sets the shared-memory attribute and returns the resident CTAs per SM (0 if it cannot run).
+int variant_prepare(int dtype, int v);
+cudaError_t launch_sort(int dtype, const LaunchParams& p);
+
+}  // namespace gqs

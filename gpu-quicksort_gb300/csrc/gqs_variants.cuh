@@ -1,0 +1,58 @@
+// Kernel variants per key type and the code that launches one. Each translation unit
+// gqs_sort_<type>.cu includes this file once for its key type.
+#pragma once
+#include "gqs_device.cuh"
+#include "gqs_launch.h"
+
+namespace gqs {
+
+template <class C>
+struct VariantOps {
+  static VariantInfo info(const char* name) {
+    VariantInfo vi;
+    vi.ncw = C::NCW;
+    vi.threads = C::NT;
+    vi.tile = C::TILE;
+    vi.chunk = C::CHUNK;
+    vi.kpt = C::KPT;
+    vi.stages = C::STAGES;
+    vi.tiny = C::TINY;
+    vi.smem = sizeof(Smem<C>);
+    vi.name = name;
+    return vi;
+  }
+  static int prepare() {
+    const size_t smem = sizeof(Smem<C>);
+    if (cudaFuncSetAttribute(persistent_kernel<C>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+        cudaSuccess)
+      return 0;
+    int blocks = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, persistent_kernel<C>, C::NT, smem) != cudaSuccess)
+      return 0;
+    return blocks;
+  }
+  static cudaError_t launch(const LaunchParams& p) {
+    using B = typename C::B;
+    SortArgs<typename C::T> a;
+    a.d = static_cast<B*>(p.d);
+    a.dn = static_cast<B*>(p.dn);
+    a.jobs = p.jobs;
+    a.q = p.q;
+    a.capacity = p.capacity;
+    a.epoch = p.epoch;
+    a.timeout_ns = p.timeout_ns;
+    const uint32_t nseg = p.offsets ? p.nseg : 1u;
+    const uint32_t seed_blocks = (nseg + 7u) / 8u;  // 8 warps per 256-thread block, one per segment
+    seed_kernel<C><<<seed_blocks, 256, 0, p.stream>>>(a, p.offsets, nseg, p.n);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    if (p.ev_begin) cudaEventRecord(p.ev_begin, p.stream);
+    persistent_kernel<C><<<p.grid, C::NT, sizeof(Smem<C>), p.stream>>>(a);
+    e = cudaGetLastError();
+    if (p.ev_end) cudaEventRecord(p.ev_end, p.stream);
+    return e;
+  }
+};
+
+}  // namespace gqs
+

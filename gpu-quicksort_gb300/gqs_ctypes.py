@@ -1,0 +1,265 @@
+"""ctypes binding of the gqs C ABI (include/gqs.h) and of the workload generators.
+
+This is the binding a Python caller of the reference's GPUQSort<T> path would add: one
+`ctypes.CDLL` over libgqs.so with the argument types declared once. The library is required;
+there is no CPU fallback, and a missing build raises immediately.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libgqs.so")
+WORKLOAD_PATH = os.path.join(HERE, "libgqs_workload.so")
+
+DTYPES = {"u32": 0, "f32": 1, "f64": 2}
+NP_DTYPES = {"u32": np.uint32, "f32": np.float32, "f64": np.float64}
+DIST = {"uniform": 0, "sorted": 1, "reverse": 2, "distinct16": 3, "zipf": 4, "gaussian": 5, "kat": 6,
+        "allequal": 7}
+
+STATUS = {0: "GQS_OK", 1: "GQS_ERR_INVALID", 2: "GQS_ERR_CUDA", 3: "GQS_ERR_NOMEM", 4: "GQS_ERR_TIMEOUT",
+          5: "GQS_ERR_CAPACITY", 6: "GQS_ERR_NO_DEVICE", 7: "GQS_ERR_INTERNAL"}
+
+# Every function include/gqs.h declares.
+EXPORTS = [
+    "gqs_config_default", "gqs_create", "gqs_destroy", "gqs_reserve",
+    "gqs_sort_u32", "gqs_sort_f32", "gqs_sort_f64",
+    "gqs_sort_u32_dev", "gqs_sort_f32_dev", "gqs_sort_f64_dev",
+    "gqs_sort_segments_u32_dev", "gqs_sort_segments_f32_dev", "gqs_sort_segments_f64_dev",
+    "gqs_sort_segments_u32", "gqs_sort_segments_f32", "gqs_sort_segments_f64",
+    "gqs_sync", "gqs_last_stats", "gqs_variant_count", "gqs_variant_describe", "gqs_set_variant",
+    "gqs_get_variant", "gqs_strerror", "gqs_version",
+]
+
+
+class GqsError(RuntimeError):
+    def __init__(self, code: int, what: str):
+        super().__init__(f"{what}: {STATUS.get(code, code)}")
+        self.code = code
+
+
+class Config(C.Structure):
+    _fields_ = [("variant", C.c_int32), ("timeout_ms", C.c_uint32), ("sync", C.c_uint32),
+                ("timing", C.c_uint32), ("reserved", C.c_uint32 * 4)]
+
+
+class Stats(C.Structure):
+    _fields_ = [("keys", C.c_uint64), ("part_keys", C.c_uint64), ("local_keys", C.c_uint64),
+                ("tiny_keys", C.c_uint64), ("fill_keys", C.c_uint64), ("chunks", C.c_uint64),
+                ("algo_bytes", C.c_uint64), ("part_jobs", C.c_uint32), ("local_jobs", C.c_uint32),
+                ("fill_chunks", C.c_uint32), ("max_depth", C.c_uint32), ("status", C.c_uint32),
+                ("variant", C.c_uint32), ("grid", C.c_uint32), ("threads", C.c_uint32),
+                ("kernel_ms", C.c_double)]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+class VariantDesc(C.Structure):
+    _fields_ = [("threads", C.c_int32), ("tile", C.c_int32), ("chunk", C.c_int32), ("kpt", C.c_int32),
+                ("stages", C.c_int32), ("tiny", C.c_int32), ("smem_bytes", C.c_uint64), ("name", C.c_char * 64)]
+
+
+_lib = None
+_wl = None
+
+
+def load_library(path: str | None = None) -> C.CDLL:
+    """Loads libgqs.so and declares its signatures (raises if it was never built)."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise FileNotFoundError(f"{p} is missing: build it with __graft_entry__.build() "
+                                "(the sort has no CPU fallback)")
+    lib = C.CDLL(p)
+    vp, sz, st = C.c_void_p, C.c_size_t, C.c_int
+    lib.gqs_config_default.argtypes = [C.POINTER(Config)]
+    lib.gqs_config_default.restype = None
+    lib.gqs_create.argtypes = [C.POINTER(vp), C.c_int, C.POINTER(Config)]
+    lib.gqs_create.restype = st
+    lib.gqs_destroy.argtypes = [vp]
+    lib.gqs_destroy.restype = None
+    lib.gqs_reserve.argtypes = [vp, C.c_int, sz, sz, C.c_int]
+    lib.gqs_reserve.restype = st
+    for t in ("u32", "f32", "f64"):
+        f = getattr(lib, f"gqs_sort_{t}")
+        f.argtypes = [vp, vp, vp, sz]
+        f.restype = st
+        f = getattr(lib, f"gqs_sort_{t}_dev")
+        f.argtypes = [vp, vp, vp, sz, vp]
+        f.restype = st
+        f = getattr(lib, f"gqs_sort_segments_{t}_dev")
+        f.argtypes = [vp, vp, vp, sz, vp, sz, vp]
+        f.restype = st
+        f = getattr(lib, f"gqs_sort_segments_{t}")
+        f.argtypes = [vp, vp, sz, vp, sz]
+        f.restype = st
+    lib.gqs_sync.argtypes = [vp]
+    lib.gqs_sync.restype = st
+    lib.gqs_last_stats.argtypes = [vp, C.POINTER(Stats)]
+    lib.gqs_last_stats.restype = st
+    lib.gqs_variant_count.argtypes = [C.c_int]
+    lib.gqs_variant_count.restype = C.c_int
+    lib.gqs_variant_describe.argtypes = [C.c_int, C.c_int, C.POINTER(VariantDesc)]
+    lib.gqs_variant_describe.restype = st
+    lib.gqs_set_variant.argtypes = [vp, C.c_int, C.c_int]
+    lib.gqs_set_variant.restype = st
+    lib.gqs_get_variant.argtypes = [vp, C.c_int]
+    lib.gqs_get_variant.restype = C.c_int
+    lib.gqs_strerror.argtypes = [C.c_int]
+    lib.gqs_strerror.restype = C.c_char_p
+    lib.gqs_version.argtypes = []
+    lib.gqs_version.restype = C.c_int
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def _check(code: int, what: str) -> None:
+    if code != 0:
+        raise GqsError(code, what)
+
+
+def _ptr(a: np.ndarray) -> int:
+    return a.ctypes.data
+
+
+class Context:
+    """A gqs context on one device (the reference's OCLResources role)."""
+
+    def __init__(self, device: int = 0, sync: bool = True, timing: bool = False, timeout_ms: int = 4000,
+                 variant: int = -1):
+        self.lib = load_library()
+        cfg = Config()
+        self.lib.gqs_config_default(C.byref(cfg))
+        cfg.sync = 1 if sync else 0
+        cfg.timing = 1 if timing else 0
+        cfg.timeout_ms = timeout_ms
+        cfg.variant = variant
+        h = C.c_void_p()
+        _check(self.lib.gqs_create(C.byref(h), device, C.byref(cfg)), "gqs_create")
+        self.h = h
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            self.lib.gqs_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # --- host pointers (the reference's GPUQSort<T>(ctx, size, d, dn)) ---
+    def sort(self, a: np.ndarray) -> None:
+        """Sorts a contiguous numpy array of uint32/float32/float64 in place."""
+        t = _np_tag(a)
+        assert a.flags.c_contiguous
+        _check(getattr(self.lib, f"gqs_sort_{t}")(self.h, _ptr(a), None, a.size), f"gqs_sort_{t}")
+
+    def sort_segments(self, a: np.ndarray, offsets: np.ndarray) -> None:
+        t = _np_tag(a)
+        off = np.ascontiguousarray(offsets, dtype=np.uint64)
+        _check(getattr(self.lib, f"gqs_sort_segments_{t}")(self.h, _ptr(a), a.size, _ptr(off), off.size - 1),
+               f"gqs_sort_segments_{t}")
+
+    # --- device pointers ---
+    def sort_dev(self, dtype: str, d: int, scratch: int | None, n: int, stream: int = 0) -> int:
+        return getattr(self.lib, f"gqs_sort_{dtype}_dev")(self.h, d, scratch, n, stream or None)
+
+    def sort_segments_dev(self, dtype: str, keys: int, scratch: int | None, n: int, offsets: int, nseg: int,
+                          stream: int = 0) -> int:
+        return getattr(self.lib, f"gqs_sort_segments_{dtype}_dev")(self.h, keys, scratch, n, offsets, nseg,
+                                                                    stream or None)
+
+    def reserve(self, dtype: str, n: int, nseg: int = 1, with_buffers: bool = False) -> None:
+        _check(self.lib.gqs_reserve(self.h, DTYPES[dtype], n, nseg, 1 if with_buffers else 0), "gqs_reserve")
+
+    def sync(self) -> int:
+        return self.lib.gqs_sync(self.h)
+
+    def stats(self) -> dict:
+        s = Stats()
+        code = self.lib.gqs_last_stats(self.h, C.byref(s))
+        d = s.as_dict()
+        d["call_status"] = code
+        return d
+
+    def set_variant(self, dtype: str, v: int) -> None:
+        _check(self.lib.gqs_set_variant(self.h, DTYPES[dtype], v), "gqs_set_variant")
+
+    def get_variant(self, dtype: str) -> int:
+        return self.lib.gqs_get_variant(self.h, DTYPES[dtype])
+
+
+def variants(dtype: str) -> list[dict]:
+    lib = load_library()
+    out = []
+    for v in range(lib.gqs_variant_count(DTYPES[dtype])):
+        d = VariantDesc()
+        _check(lib.gqs_variant_describe(DTYPES[dtype], v, C.byref(d)), "gqs_variant_describe")
+        out.append({"index": v, "threads": d.threads, "tile": d.tile, "chunk": d.chunk, "kpt": d.kpt,
+                    "stages": d.stages, "tiny": d.tiny, "smem_bytes": d.smem_bytes, "name": d.name.decode()})
+    return out
+
+
+def _np_tag(a: np.ndarray) -> str:
+    for t, dt in NP_DTYPES.items():
+        if a.dtype == dt:
+            return t
+    raise TypeError(f"unsupported key dtype {a.dtype}")
+
+
+# ---------------------------------------------------------------------------
+# Workload generators (libgqs_workload.so)
+
+def load_workload() -> C.CDLL:
+    global _wl
+    if _wl is not None:
+        return _wl
+    if not os.path.exists(WORKLOAD_PATH):
+        raise FileNotFoundError(f"{WORKLOAD_PATH} is missing: build it with __graft_entry__.build()")
+    wl = C.CDLL(WORKLOAD_PATH)
+    for t in ("u32", "f32", "f64"):
+        f = getattr(wl, f"gqs_workload_{t}")
+        f.argtypes = [C.c_int, C.c_uint64, C.c_size_t, C.c_void_p]
+        f.restype = C.c_int
+    wl.gqs_workload_segments.argtypes = [C.c_uint64, C.c_size_t, C.c_uint64, C.c_uint64, C.c_void_p]
+    wl.gqs_workload_segments.restype = C.c_uint64
+    for name in ("gqs_workload_det_log", "gqs_workload_det_exp", "gqs_workload_det_cos2pi"):
+        getattr(wl, name).argtypes = [C.c_double]
+        getattr(wl, name).restype = C.c_double
+    _wl = wl
+    return wl
+
+
+def generate(dtype: str, dist: str, seed: int, n: int, out: np.ndarray | None = None) -> np.ndarray:
+    """Seeded keys of one configured distribution (identical on every platform)."""
+    wl = load_workload()
+    if out is None:
+        out = np.empty(n, dtype=NP_DTYPES[dtype])
+    assert out.dtype == NP_DTYPES[dtype] and out.size >= n and out.flags.c_contiguous
+    rc = getattr(wl, f"gqs_workload_{dtype}")(DIST[dist], seed, n, _ptr(out))
+    if rc != 0:
+        raise ValueError(f"distribution {dist} is not defined for {dtype}")
+    return out
+
+
+def segment_offsets(seed: int, nseg: int, minlen: int, maxlen: int) -> np.ndarray:
+    """nseg + 1 offsets with log-uniform segment lengths in [minlen, maxlen]."""
+    wl = load_workload()
+    off = np.empty(nseg + 1, dtype=np.uint64)
+    wl.gqs_workload_segments(seed, nseg, minlen, maxlen, _ptr(off))
+    return off

@@ -1,0 +1,139 @@
+/*
+ * gqs -- GPU-Quicksort for NVIDIA GB300 (sm_103a): the C ABI.
+ *
+ * This is the drop-in boundary for the reference's single-array sort,
+ * rioffe/gpu-quicksort `template <class T> void GPUQSort(OCLResources*, size_t size, T* d, T* dn)`
+ * (GPU-Quicksort_Full_SYCL/QuicksortMain.cpp:835-906; uint-only form at
+ * GPU-Quicksort_OpenCL_1.2/QuicksortMain.cpp:297-384), which its benchmark driver calls as
+ * GPUQSort(&myOCL, arraySize, pArray, pArrayCopy) (GPU-Quicksort_Full_SYCL/QuicksortMain.cpp:1114).
+ * The reference is C++ templates only; these plain-C entry points are what an FFI
+ * (ctypes, cgo, JNI) binds, and include/gqs/Quicksort.h restores the template.
+ *
+ * Conventions
+ *   - Every call returns a gqs_status. Nothing here calls exit(), abort() or traps; device-side
+ *     failures (a bounded wait that ran out, a full job queue) come back as a status.
+ *   - Keys: uint32_t, float, double. Output is ascending and identical to std::sort for inputs
+ *     without NaN; -0.0 sorts before +0.0 (both are kept bit for bit).
+ *   - A gqs_ctx is bound to one device. Calls on one context are serialised (internally
+ *     locked, and device work of consecutive calls is ordered even across streams). Use one
+ *     context per concurrent stream for overlap.
+ *   - Nothing is allocated on the device-pointer path once the context's pools have grown to
+ *     the largest size seen (first call at a new size allocates; gqs_reserve pre-grows).
+ */
+#ifndef GQS_H
+#define GQS_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct gqs_ctx gqs_ctx;
+
+typedef enum gqs_status {
+  GQS_OK = 0,
+  GQS_ERR_INVALID = 1,   /* null / misaligned pointer, size out of range, bad segment table */
+  GQS_ERR_CUDA = 2,      /* a CUDA runtime call failed */
+  GQS_ERR_NOMEM = 3,     /* device or pinned allocation failed */
+  GQS_ERR_TIMEOUT = 4,   /* a bounded device-side wait ran out (the sort made no progress) */
+  GQS_ERR_CAPACITY = 5,  /* the device job queue overflowed (pathological pivot sequence) */
+  GQS_ERR_NO_DEVICE = 6, /* no usable CUDA device, or not an sm_103 GPU */
+  GQS_ERR_INTERNAL = 7   /* an internal invariant failed on the device */
+} gqs_status;
+
+typedef enum gqs_dtype { GQS_U32 = 0, GQS_F32 = 1, GQS_F64 = 2 } gqs_dtype;
+
+typedef struct gqs_config {
+  int32_t variant;     /* -1: the context's tuned choice per key type; else a variant index */
+  uint32_t timeout_ms; /* device-side no-progress limit for bounded waits; 0 means 4000 */
+  uint32_t sync;       /* 1 (default): *_dev calls wait for the stream and return the device status */
+  uint32_t timing;     /* 1: time the persistent kernel with CUDA events (gqs_stats.kernel_ms) */
+  uint32_t reserved[4];
+} gqs_config;
+
+typedef struct gqs_stats {
+  uint64_t keys;       /* keys in the last sort */
+  uint64_t part_keys;  /* keys read by partition chunks, summed over all levels */
+  uint64_t local_keys; /* keys sorted on chip by local jobs */
+  uint64_t tiny_keys;  /* keys sorted in registers by a single warp */
+  uint64_t fill_keys;  /* pivot-run keys written by the completer warp */
+  uint64_t chunks;     /* partition chunks processed */
+  uint64_t algo_bytes; /* key bytes * 2 * (part_keys + local_keys + tiny_keys) */
+  uint32_t part_jobs, local_jobs, fill_chunks, max_depth;
+  uint32_t status, variant, grid, threads;
+  double kernel_ms; /* persistent-kernel time from CUDA events, or -1 when timing is off */
+} gqs_stats;
+
+typedef struct gqs_variant_desc {
+  int32_t threads, tile, chunk, kpt, stages, tiny;
+  uint64_t smem_bytes;
+  char name[64];
+} gqs_variant_desc;
+
+/* Fills *cfg with the defaults (variant -1, timeout 4000 ms, sync 1, timing 0). */
+void gqs_config_default(gqs_config* cfg);
+
+/* Creates a context on `device` (cfg may be NULL for the defaults). */
+gqs_status gqs_create(gqs_ctx** out, int device, const gqs_config* cfg);
+void gqs_destroy(gqs_ctx* ctx);
+
+/* Pre-grows the context's pools for n keys of `dtype` in up to `nseg` segments, so later
+ * calls of that size allocate nothing. with_buffers also sizes the key/scratch pools that the
+ * host-pointer calls stage through. */
+gqs_status gqs_reserve(gqs_ctx* ctx, int dtype, size_t n, size_t nseg, int with_buffers);
+
+/* Host-pointer sorts, the reference's semantics: `d` (host memory, n keys) is sorted in place.
+ * `dn` is the reference's scratch array; it is not touched and may be NULL (device scratch
+ * comes from the context pool). Keys travel over one host->device and one device->host copy
+ * (fastest from pinned memory). Replaces GPUQSort<T>(OCLResources*, size, d, dn),
+ * GPU-Quicksort_Full_SYCL/QuicksortMain.cpp:835-836. */
+gqs_status gqs_sort_u32(gqs_ctx* ctx, uint32_t* d, uint32_t* dn, size_t n);
+gqs_status gqs_sort_f32(gqs_ctx* ctx, float* d, float* dn, size_t n);
+gqs_status gqs_sort_f64(gqs_ctx* ctx, double* d, double* dn, size_t n);
+
+/* Device-pointer sorts: `d` (device memory, n keys) is sorted in place; `scratch` is n keys of
+ * device memory clobbered by the sort (the reference's dn), or NULL to use the context pool.
+ * Work is ordered on `stream` (a cudaStream_t; NULL = legacy default stream). With
+ * cfg.sync = 1 the call waits and returns the device status; with sync = 0 it returns after
+ * enqueueing and gqs_sync() reports the device status. Same replacement as above, with the
+ * buffers already resident in HBM. */
+gqs_status gqs_sort_u32_dev(gqs_ctx* ctx, uint32_t* d, uint32_t* scratch, size_t n, void* stream);
+gqs_status gqs_sort_f32_dev(gqs_ctx* ctx, float* d, float* scratch, size_t n, void* stream);
+gqs_status gqs_sort_f64_dev(gqs_ctx* ctx, double* d, double* scratch, size_t n, void* stream);
+
+/* Segmented sorts: keys[offsets[i], offsets[i+1]) is sorted independently for each of the
+ * nseg segments, all in one persistent launch. offsets holds nseg + 1 non-decreasing entries
+ * (device memory for *_dev, host memory otherwise) with offsets[nseg] <= n, where n is the
+ * length of keys (and of scratch). No reference counterpart: the reference sorts one array per
+ * call; this is the batched form of the same GPUQSort<T> path. */
+gqs_status gqs_sort_segments_u32_dev(gqs_ctx* ctx, uint32_t* keys, uint32_t* scratch, size_t n,
+                                     const uint64_t* offsets, size_t nseg, void* stream);
+gqs_status gqs_sort_segments_f32_dev(gqs_ctx* ctx, float* keys, float* scratch, size_t n,
+                                     const uint64_t* offsets, size_t nseg, void* stream);
+gqs_status gqs_sort_segments_f64_dev(gqs_ctx* ctx, double* keys, double* scratch, size_t n,
+                                     const uint64_t* offsets, size_t nseg, void* stream);
+gqs_status gqs_sort_segments_u32(gqs_ctx* ctx, uint32_t* keys, size_t n, const uint64_t* offsets, size_t nseg);
+gqs_status gqs_sort_segments_f32(gqs_ctx* ctx, float* keys, size_t n, const uint64_t* offsets, size_t nseg);
+gqs_status gqs_sort_segments_f64(gqs_ctx* ctx, double* keys, size_t n, const uint64_t* offsets, size_t nseg);
+
+/* Waits for the context's last enqueued sort and returns its device status. */
+gqs_status gqs_sync(gqs_ctx* ctx);
+
+/* Statistics of the last completed sort (waits for it if it is still running). */
+gqs_status gqs_last_stats(gqs_ctx* ctx, gqs_stats* out);
+
+/* Kernel variants available for a key type, and the one the context currently uses. */
+int gqs_variant_count(int dtype);
+gqs_status gqs_variant_describe(int dtype, int variant, gqs_variant_desc* out);
+gqs_status gqs_set_variant(gqs_ctx* ctx, int dtype, int variant);
+int gqs_get_variant(gqs_ctx* ctx, int dtype);
+
+const char* gqs_strerror(gqs_status s);
+int gqs_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GQS_H */

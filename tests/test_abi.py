@@ -1,0 +1,45 @@
+"""The C ABI library loads and exports every function include/gqs.h declares (no GPU needed)."""
+import ctypes
+import os
+import re
+
+import gqs_ctypes
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    text = open(os.path.join(ROOT, "include", "gqs.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(gqs_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_header_and_binding_agree():
+    assert declared_functions() == sorted(gqs_ctypes.EXPORTS)
+
+
+def test_library_exports_every_declared_symbol():
+    lib = gqs_ctypes.load_library()
+    for name in declared_functions():
+        assert hasattr(lib, name), name
+
+
+def test_host_only_calls():
+    lib = gqs_ctypes.load_library()
+    assert lib.gqs_version() >= 1
+    assert lib.gqs_strerror(0) == b"ok"
+    assert lib.gqs_strerror(4).startswith(b"device wait timed out")
+    cfg = gqs_ctypes.Config()
+    lib.gqs_config_default(ctypes.byref(cfg))
+    assert cfg.variant == -1 and cfg.sync == 1 and cfg.timeout_ms == 4000
+    for t in ("u32", "f32", "f64"):
+        vs = gqs_ctypes.variants(t)
+        assert vs and all(v["smem_bytes"] <= 232448 for v in vs)
+        assert all(v["tile"] > v["tiny"] for v in vs)
+
+
+def test_null_context_is_rejected():
+    lib = gqs_ctypes.load_library()
+    assert lib.gqs_sort_u32(None, None, None, 10) == 1
+    assert lib.gqs_sort_u32_dev(None, None, None, 10, None) == 1
+    assert lib.gqs_sync(None) == 1

@@ -1,0 +1,209 @@
+"""GPU parity: the CUDA sort through the C ABI against the oracle, bit for bit.
+
+Small and medium sizes compare with std::sort (the reference's verifier, run by the oracle
+library) and with the committed golden vectors; full configuration sizes compare with an
+independent GPU sort (torch.sort) and check size-independent properties (sortedness, a
+permutation-invariant checksum).
+"""
+import hashlib
+import json
+import os
+
+import numpy as np
+import pytest
+
+import gqs_ctypes
+import oracle_ctypes
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "golden.json")))["cases"]
+DISTS = {
+    "u32": ["uniform", "sorted", "reverse", "distinct16", "zipf", "gaussian", "kat", "allequal"],
+    "f32": ["gaussian", "uniform", "sorted", "reverse", "distinct16", "kat", "allequal"],
+    "f64": ["uniform", "gaussian", "sorted", "reverse", "distinct16", "kat", "allequal"],
+}
+# sizes around the register sort (256), the chunk grid, the on-chip tile, and the first levels
+SIZES = [2, 3, 31, 32, 33, 255, 256, 257, 1000, 2047, 2048, 2049, 4095, 4096, 4097, 8191, 8193, 16383,
+         16384, 16385, 32769, 100_003, 1 << 20]
+
+
+def sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def oracle_sorted(a):
+    r = a.copy()
+    oracle_ctypes.std_sort(r)
+    return r
+
+
+@pytest.mark.parametrize("dtype", ["u32", "f32", "f64"])
+@pytest.mark.parametrize("n", SIZES)
+def test_sizes_match_oracle(gpu_ctx, dtype, n):
+    for dist in ("uniform", "distinct16", "reverse"):
+        a = gqs_ctypes.generate(dtype, dist, 1000 + n, n)
+        b = a.copy()
+        gpu_ctx.sort(b)
+        assert np.array_equal(b.view(np.uint8), oracle_sorted(a).view(np.uint8)), (dtype, dist, n)
+
+
+@pytest.mark.parametrize("dtype", ["u32", "f32", "f64"])
+def test_distributions_match_oracle(gpu_ctx, dtype):
+    for dist in DISTS[dtype]:
+        for n in (5000, 70_001, 1_000_003):
+            a = gqs_ctypes.generate(dtype, dist, 77, n)
+            b = a.copy()
+            gpu_ctx.sort(b)
+            assert np.array_equal(b.view(np.uint8), oracle_sorted(a).view(np.uint8)), (dtype, dist, n)
+
+
+@pytest.mark.parametrize("case", [c for c in GOLDEN if c["n"] >= 1000],
+                         ids=lambda c: f"{c['dtype']}-{c['dist']}-{c['n']}")
+def test_golden_vectors(gpu_ctx, case):
+    a = gqs_ctypes.generate(case["dtype"], case["dist"], case["seed"], case["n"])
+    assert sha(a) == case["input_sha256"]
+    gpu_ctx.sort(a)
+    assert sha(a) == case["sorted_sha256"]
+
+
+@pytest.mark.parametrize("dtype", ["u32", "f32", "f64"])
+def test_known_answer(gpu_ctx, dtype):
+    for n in (1, 2, 1024, 1 << 16, 1 << 20, 3_000_000):
+        a = gqs_ctypes.generate(dtype, "kat", 5, n)
+        gpu_ctx.sort(a)
+        assert np.array_equal(a, np.arange(1, n + 1, dtype=a.dtype))
+
+
+def test_oracle_restatement_agrees(gpu_ctx):
+    for dtype in ("u32", "f32", "f64"):
+        a = gqs_ctypes.generate(dtype, "gaussian", 3, 1 << 18)
+        b, c = a.copy(), a.copy()
+        gpu_ctx.sort(b)
+        oracle_ctypes.gpuqsort(c, threads=8)
+        assert np.array_equal(b.view(np.uint8), c.view(np.uint8))
+
+
+def test_signed_zero_and_extremes(gpu_ctx):
+    """-0.0 sorts before +0.0 (std::sort may order them either way); every bit is kept."""
+    vals = np.array([0.0, -0.0, 1.5, -1.5, np.finfo(np.float32).max, -np.finfo(np.float32).max,
+                     np.finfo(np.float32).tiny, -np.finfo(np.float32).tiny, np.inf, -np.inf], dtype=np.float32)
+    a = np.tile(vals, 5000)
+    rng = np.random.default_rng(0)
+    rng.shuffle(a)
+    b = a.copy()
+    gpu_ctx.sort(b)
+    expect = np.sort(a)
+    assert np.array_equal(b, expect)  # value order
+    zeros = b[b == 0]
+    nneg = int(np.sum(np.signbit(a) & (a == 0)))
+    assert np.all(np.signbit(zeros[:nneg])) and not np.any(np.signbit(zeros[nneg:]))
+    u = np.array([0, 1, 0xFFFFFFFF, 0x80000000, 0x7FFFFFFF] * 4000, dtype=np.uint32)
+    rng.shuffle(u)
+    v = u.copy()
+    gpu_ctx.sort(v)
+    assert np.array_equal(v, np.sort(u))
+
+
+def test_repeated_calls_reuse_context(gpu_ctx):
+    a = gqs_ctypes.generate("u32", "uniform", 99, 1 << 20)
+    ref = oracle_sorted(a)
+    for _ in range(5):
+        b = a.copy()
+        gpu_ctx.sort(b)
+        assert np.array_equal(b, ref)
+    st = gpu_ctx.stats()
+    assert st["status"] == 0 and st["keys"] == 1 << 20
+    assert st["part_keys"] + st["local_keys"] + st["tiny_keys"] >= 1 << 20
+
+
+# ---------------------------------------------------------------------------
+# device pointers (torch supplies HBM buffers and the stream)
+
+def _torch():
+    return pytest.importorskip("torch")
+
+
+@pytest.mark.parametrize("dtype", ["u32", "f32", "f64"])
+@pytest.mark.parametrize("shift", [0, 1, 3])
+def test_device_api_unaligned_views(gpu_ctx, dtype, shift):
+    torch = _torch()
+    tdt = {"u32": torch.int32, "f32": torch.float32, "f64": torch.float64}[dtype]
+    n = 1_000_001
+    a = gqs_ctypes.generate(dtype, "uniform" if dtype != "f32" else "gaussian", 8, n)
+    host = torch.from_numpy(a.view(np.int32) if dtype == "u32" else a)
+    buf = torch.empty(n + 8, dtype=tdt, device="cuda")
+    scr = torch.empty(n + 8, dtype=tdt, device="cuda")
+    d = buf[shift:shift + n]
+    d.copy_(host)
+    s = scr[(shift + 1) % 4:(shift + 1) % 4 + n]  # scratch misaligned differently from d
+    stream = torch.cuda.current_stream().cuda_stream
+    rc = gpu_ctx.sort_dev(dtype, d.data_ptr(), s.data_ptr(), n, stream)
+    assert rc == 0
+    out = d.cpu().numpy()
+    if dtype == "u32":
+        out = out.view(np.uint32)
+    assert np.array_equal(out.view(np.uint8), oracle_sorted(a).view(np.uint8))
+
+
+def test_device_api_guard_words_untouched(gpu_ctx):
+    torch = _torch()
+    n = 300_007
+    a = gqs_ctypes.generate("u32", "uniform", 12, n)
+    buf = torch.full((n + 64,), -7, dtype=torch.int32, device="cuda")
+    d = buf[32:32 + n]
+    d.copy_(torch.from_numpy(a.view(np.int32)))
+    assert gpu_ctx.sort_dev("u32", d.data_ptr(), None, n, torch.cuda.current_stream().cuda_stream) == 0
+    host = buf.cpu().numpy()
+    assert np.all(host[:32] == -7) and np.all(host[32 + n:] == -7)
+    assert np.array_equal(host[32:32 + n].view(np.uint32), np.sort(a))
+
+
+def test_async_calls_then_sync():
+    torch = _torch()
+    ctx = gqs_ctypes.Context(sync=False, timing=True)
+    try:
+        n = 1 << 22
+        a = gqs_ctypes.generate("u32", "uniform", 13, n)
+        ref = np.sort(a)
+        bufs = [torch.from_numpy(a.view(np.int32)).cuda() for _ in range(3)]
+        side = torch.cuda.Stream()
+        for i, b in enumerate(bufs):
+            st = side if i == 1 else torch.cuda.current_stream()
+            assert ctx.sort_dev("u32", b.data_ptr(), None, n, st.cuda_stream) == 0
+        assert ctx.sync() == 0
+        torch.cuda.synchronize()
+        for b in bufs:
+            assert np.array_equal(b.cpu().numpy().view(np.uint32), ref)
+        st = ctx.stats()
+        assert st["kernel_ms"] > 0
+    finally:
+        ctx.close()
+
+
+# ---------------------------------------------------------------------------
+# full configuration sizes: exact comparison with an independent GPU sort
+
+FULL = [("u32", d, 1 << 28) for d in ("uniform", "sorted", "reverse", "distinct16", "zipf", "gaussian")] + [
+    ("f32", "gaussian", 1 << 27), ("f64", "uniform", 1 << 26)]
+
+
+@pytest.mark.parametrize("dtype,dist,n", FULL, ids=lambda x: str(x))
+def test_full_size_configs(gpu_ctx, dtype, dist, n):
+    torch = _torch()
+    a = gqs_ctypes.generate(dtype, dist, 2026, n)
+    if dtype == "u32":
+        t = torch.from_numpy(a.view(np.int32)).cuda()
+        ref = torch.sort(t.to(torch.int64) & 0xFFFFFFFF).values
+    else:
+        t = torch.from_numpy(a).cuda()
+        ref = torch.sort(t).values
+    assert gpu_ctx.sort_dev(dtype, t.data_ptr(), None, n, torch.cuda.current_stream().cuda_stream) == 0
+    got = (t.to(torch.int64) & 0xFFFFFFFF) if dtype == "u32" else t
+    assert torch.equal(got, ref)
+    # size-independent properties on top of the exact comparison
+    assert bool((got[1:] >= got[:-1]).all())
+    st = gpu_ctx.stats()
+    assert st["status"] == 0 and st["keys"] == n
+    del t, ref, got
+    torch.cuda.empty_cache()
