@@ -52,6 +52,7 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-clocks", action="store_true")
+    p.add_argument("--profile", action="store_true", help="use libgqs_prof.so and print its cycle counters")
     return p.parse_args()
 
 
@@ -199,6 +200,9 @@ def main():
     if args.impl == "reference":
         run_reference(args)
         return
+    if args.profile:
+        import build_lib
+        os.environ["GQS_LIB"] = build_lib.build(profile=True)["lib"]
     import torch
     import gqs_ctypes
 
@@ -355,6 +359,7 @@ def main():
         "stats": {k: stats_last[k] for k in ("part_keys", "local_keys", "tiny_keys", "fill_keys", "chunks",
                                              "part_jobs", "local_jobs", "fill_chunks", "max_depth")},
         "passes_per_key": (stats_last["part_keys"] + stats_last["local_keys"] + stats_last["tiny_keys"]) / n,
+        "profile": ctx.profile() if args.profile else None,
         "wall_s": wall,
     }
     print(json.dumps(line), flush=True)

@@ -26,6 +26,7 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompil
 CU_SOURCES = ["gqs_sort_u32.cu", "gqs_sort_f32.cu", "gqs_sort_f64.cu", "gqs_capi.cu"]
 
 LIB = os.path.join(HERE, "libgqs.so")
+PROF_LIB = os.path.join(HERE, "libgqs_prof.so")  # -DGQS_PROFILE: per-role cycle counters
 WORKLOAD_LIB = os.path.join(HERE, "libgqs_workload.so")
 
 
@@ -55,19 +56,23 @@ def _headers() -> list[str]:
     return hs
 
 
-def build(force: bool = False, verbose: bool = False) -> dict:
-    """Compiles what is out of date; returns the library paths."""
-    os.makedirs(BUILD, exist_ok=True)
+def build(force: bool = False, verbose: bool = False, profile: bool = False) -> dict:
+    """Compiles what is out of date; returns the library paths. profile=True builds
+    libgqs_prof.so with the device cycle counters instead of libgqs.so."""
+    bdir = BUILD + ("_prof" if profile else "")
+    lib = PROF_LIB if profile else LIB
+    extra = ["-DGQS_PROFILE"] if profile else []
+    os.makedirs(bdir, exist_ok=True)
     nvcc = _nvcc()
     headers = _headers()
     jobs = []
     objs = []
     for src in CU_SOURCES:
         s = os.path.join(CSRC, src)
-        o = os.path.join(BUILD, src.replace(".cu", ".o"))
+        o = os.path.join(bdir, src.replace(".cu", ".o"))
         objs.append(o)
         if force or _stale(o, [s] + headers):
-            jobs.append([nvcc] + ARCH + NVCC_FLAGS + ["-c", s, "-o", o])
+            jobs.append([nvcc] + ARCH + NVCC_FLAGS + extra + ["-c", s, "-o", o])
     wsrc = os.path.join(HERE, "workload", "gqs_workload.cpp")
     whdr = os.path.join(HERE, "workload", "gqs_workload.h")
     wjob = None
@@ -80,12 +85,12 @@ def build(force: bool = False, verbose: bool = False) -> dict:
             futs.append(ex.submit(_run, wjob))
         for f in futs:
             f.result()
-    if force or jobs or _stale(LIB, objs):
-        _run([nvcc] + ARCH + ["-shared", "-o", LIB] + objs + ["-Xcompiler", "-fPIC"])
+    if force or jobs or _stale(lib, objs):
+        _run([nvcc] + ARCH + ["-shared", "-o", lib] + objs + ["-Xcompiler", "-fPIC"])
     if verbose:
-        print("built", LIB, WORKLOAD_LIB)
-    return {"lib": LIB, "workload": WORKLOAD_LIB}
+        print("built", lib, WORKLOAD_LIB)
+    return {"lib": lib, "workload": WORKLOAD_LIB}
 
 
 if __name__ == "__main__":
-    build(force="--force" in sys.argv, verbose=True)
+    build(force="--force" in sys.argv, verbose=True, profile="--profile" in sys.argv)

@@ -86,7 +86,8 @@ struct gqs_ctx {
   gqs::Queue* q_host = nullptr;  // pinned
   unsigned long long* offs = nullptr;
   size_t offs_cap = 0;
-  uint32_t epoch = 0;
+  unsigned long long* tmap = nullptr;  // ticket ring
+  size_t tmap_len = 0;                 // entries (a power of two)
   cudaEvent_t ev_begin = nullptr, ev_end = nullptr, ev_done = nullptr;
   bool pending = false;
   bool pending_timed = false;
@@ -95,6 +96,7 @@ struct gqs_ctx {
   int pending_grid = 0;
   unsigned long long pending_keys = 0;
   gqs_stats last{};
+  uint64_t last_prof[32] = {};
   int variant[3] = {0, 0, 0};
   int blocks_per_sm[3][kMaxVariants] = {};
 };
@@ -131,6 +133,16 @@ size_t job_capacity(const gqs::VariantInfo& vi, size_t n, size_t nseg) {
   return n / (size_t)vi.tiny + 16 * (n / (size_t)vi.tile) + n / 32768 + 2 * nseg + 4096;
 }
 
+// Ticket-ring entries: tickets not yet taken belong to live jobs, whose ranges are disjoint,
+// so they number at most the chunks of n keys (plus one partial chunk per job) plus one per
+// local job and fill chunk.
+size_t ticket_ring(const gqs::VariantInfo& vi, size_t n, size_t nseg) {
+  size_t need = 2 * (n / (size_t)vi.chunk) + n / (size_t)vi.tiny + n / 32768 + 2 * nseg + 65536;
+  size_t r = 1;
+  while (r < need) r <<= 1;
+  return r;
+}
+
 gqs_status wait_pending_locked(gqs_ctx* c) {
   if (!c->pending) return GQS_OK;
   cudaError_t e = cudaEventSynchronize(c->ev_done);
@@ -162,6 +174,7 @@ gqs_status wait_pending_locked(gqs_ctx* c) {
   }
   if (q.error == 0 && q.done != q.total) s.status = GQS_ERR_INTERNAL;
   c->last = s;
+  for (int i = 0; i < 32; ++i) c->last_prof[i] = q.prof[i];
   return (gqs_status)s.status;
 }
 
@@ -175,7 +188,8 @@ gqs_status enqueue_locked(gqs_ctx* c, int dtype, void* d, void* dn, size_t n, co
   const int v = c->variant[dtype];
   const gqs::VariantInfo vi = gqs::variant_info(dtype, v);
   const size_t cap = job_capacity(vi, n, nseg);
-  if (cap >= (1ull << 32)) return GQS_ERR_INVALID;
+  const size_t ring = ticket_ring(vi, n, nseg);
+  if (cap >= (1ull << 32) || ring > (1ull << 31)) return GQS_ERR_INVALID;
   if (!c->blocks_per_sm[dtype][v]) {
     c->blocks_per_sm[dtype][v] = gqs::variant_prepare(dtype, v);
     if (!c->blocks_per_sm[dtype][v]) return GQS_ERR_NO_DEVICE;
@@ -183,7 +197,8 @@ gqs_status enqueue_locked(gqs_ctx* c, int dtype, void* d, void* dn, size_t n, co
   gqs_status st = GQS_OK;
   const bool need_jobs = c->job_cap < cap;
   const bool need_dn = !dn && c->pool_dn_bytes < n * es;
-  if (need_jobs || need_dn) {
+  const bool need_ring = c->tmap_len < ring;
+  if (need_jobs || need_dn || need_ring) {
     st = wait_pending_locked(c);
     if (st != GQS_OK && st != GQS_ERR_TIMEOUT && st != GQS_ERR_CAPACITY && st != GQS_ERR_INTERNAL) return st;
     size_t bytes = 0;
@@ -194,9 +209,14 @@ gqs_status enqueue_locked(gqs_ctx* c, int dtype, void* d, void* dn, size_t n, co
       c->jobs = static_cast<gqs::Job*>(p);
       c->job_cap = c->jobs ? bytes / sizeof(gqs::Job) : 0;
       if (st != GQS_OK) return st;
-      // fresh records must not carry a stale epoch
-      cudaError_t e = cudaMemset(c->jobs, 0, c->job_cap * sizeof(gqs::Job));
-      if (e != cudaSuccess) return cuda_status(e);
+    }
+    if (need_ring) {
+      void* p = c->tmap;
+      size_t bytes = c->tmap_len * sizeof(unsigned long long);
+      st = grow(&p, &bytes, ring * sizeof(unsigned long long));
+      c->tmap = static_cast<unsigned long long*>(p);
+      c->tmap_len = c->tmap ? ring : 0;
+      if (st != GQS_OK) return st;
     }
     if (need_dn) {
       st = grow(&c->pool_dn, &c->pool_dn_bytes, n * es);
@@ -210,18 +230,17 @@ gqs_status enqueue_locked(gqs_ctx* c, int dtype, void* d, void* dn, size_t n, co
   }
   cudaError_t e = cudaMemsetAsync(c->q, 0, sizeof(gqs::Queue), stream);
   if (e != cudaSuccess) return cuda_status(e);
-  if (++c->epoch == 0) {
-    c->epoch = 1;
-    e = cudaMemsetAsync(c->jobs, 0, c->job_cap * sizeof(gqs::Job), stream);
-    if (e != cudaSuccess) return cuda_status(e);
-  }
+  // Only the part of the ring this sort can reach needs clearing.
+  e = cudaMemsetAsync(c->tmap, 0, ring * sizeof(unsigned long long), stream);
+  if (e != cudaSuccess) return cuda_status(e);
   gqs::LaunchParams p{};
   p.d = d;
   p.dn = dn;
   p.jobs = c->jobs;
   p.q = c->q;
+  p.tmap = c->tmap;
   p.capacity = (uint32_t)c->job_cap;
-  p.epoch = c->epoch;
+  p.tmask = (uint32_t)(ring - 1);
   p.timeout_ns = (unsigned long long)(c->cfg.timeout_ms ? c->cfg.timeout_ms : 4000) * 1000000ull;
   p.offsets = offsets;
   p.n = n;
@@ -394,6 +413,7 @@ void gqs_destroy(gqs_ctx* c) {
     if (c->jobs) cudaFree(c->jobs);
     if (c->q) cudaFree(c->q);
     if (c->offs) cudaFree(c->offs);
+    if (c->tmap) cudaFree(c->tmap);
     if (c->q_host) cudaFreeHost(c->q_host);
     if (c->ev_begin) cudaEventDestroy(c->ev_begin);
     if (c->ev_end) cudaEventDestroy(c->ev_end);
@@ -422,7 +442,15 @@ gqs_status gqs_reserve(gqs_ctx* c, int dtype, size_t n, size_t nseg, int with_bu
     c->jobs = static_cast<gqs::Job*>(p);
     c->job_cap = c->jobs ? bytes / sizeof(gqs::Job) : 0;
     if (st != GQS_OK) return st;
-    if (cudaMemset(c->jobs, 0, c->job_cap * sizeof(gqs::Job)) != cudaSuccess) return GQS_ERR_CUDA;
+  }
+  const size_t ring = ticket_ring(vi, n, nseg ? nseg : 1);
+  if (c->tmap_len < ring) {
+    void* p = c->tmap;
+    size_t bytes = c->tmap_len * sizeof(unsigned long long);
+    gqs_status st = grow(&p, &bytes, ring * sizeof(unsigned long long));
+    c->tmap = static_cast<unsigned long long*>(p);
+    c->tmap_len = c->tmap ? ring : 0;
+    if (st != GQS_OK) return st;
   }
   const size_t bytes = n * kElemSize[dtype];
   gqs_status st = grow(&c->pool_dn, &c->pool_dn_bytes, bytes);
@@ -489,6 +517,16 @@ gqs_status gqs_last_stats(gqs_ctx* c, gqs_stats* out) {
   gqs_status st = wait_pending_locked(c);
   *out = c->last;
   return st == GQS_OK ? GQS_OK : st;
+}
+
+int gqs_last_profile(gqs_ctx* c, uint64_t* out, size_t n) {
+  if (!c || !out) return 0;
+  std::lock_guard<std::mutex> lk(c->mu);
+  DeviceGuard dg(c->device);
+  (void)wait_pending_locked(c);
+  const size_t k = n < 32 ? n : 32;
+  for (size_t i = 0; i < k; ++i) out[i] = c->last_prof[i];
+  return (int)k;
 }
 
 int gqs_variant_count(int dtype) { return gqs::variant_count(dtype); }

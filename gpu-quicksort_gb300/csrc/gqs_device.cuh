@@ -36,26 +36,73 @@ enum : uint32_t { ITEM_PART = 1, ITEM_LOCAL = 2, ITEM_FILL = 3, ITEM_TERM = 4, I
 // One queued unit of work. A partition job covers [start, end) of its source buffer and is
 // cut into chunks on a grid aligned to 16 bytes of the source; its children are written
 // to the other buffer. `dir` follows the reference's `direction`: 1 reads d, 0 reads dn.
+// Every chunk of every job owns one ticket; tickets [t0, t0 + nchunks) belong to this job.
 struct alignas(16) Job {
   unsigned long long start, end;
   unsigned long long sstart, send;  // reservation cursors: less-than grows up, greater-than down
   unsigned long long pivot;         // comparison key of the pivot
   long long grid;                   // element index of the chunk grid origin (may be < start)
-  uint32_t kind, dir, nchunks, cursor;
-  uint32_t remaining, depth, ready, pad;
+  uint32_t kind, dir, nchunks, t0;
+  uint32_t remaining, depth, pad0, pad1;
 };
 static_assert(sizeof(Job) == 80, "job record layout");
 
 // Per-sort device state. Reset by the host (memset) before the seed kernel.
+// Work is handed out by ticket: `grab` counts tickets taken, the low half of `alloc` counts
+// tickets created and its high half job records created. The ticket map (SortArgs::tmap)
+// holds ((ticket + 1) << 32 | job slot) at index ticket & tmask once the job is published.
 struct Queue {
   unsigned long long total;  // keys in this sort
   unsigned long long done;   // keys in their final place
-  uint32_t head, tail;       // first job with chunks left to take; jobs allocated
-  uint32_t error, pad0;
+  unsigned long long alloc;  // (jobs << 32) | tickets
+  uint32_t grab, error;
   unsigned long long error_info;
   unsigned long long part_keys, local_keys, tiny_keys, fill_keys, chunks;
   uint32_t part_jobs, local_jobs, fill_jobs, max_depth;
+  unsigned long long prof[32];  // cycle counters of a -DGQS_PROFILE build (zero otherwise)
 };
+
+// Optional cycle accounting per role (compile with -DGQS_PROFILE); slots:
+enum : int {
+  PF_C_WAIT = 0,     // consumer leader: waiting for the next ring slot
+  PF_C_PART = 1,     // consumers: partition chunk iterations
+  PF_C_DRAIN = 2,    // consumers: draining before a non-partition item
+  PF_C_LWAIT = 3,    // consumers: waiting for a local tile
+  PF_C_LCTA = 4,     // local sort, CTA-wide phase (incl. key mapping)
+  PF_C_LWARP = 5,    // local sort, warp phase
+  PF_C_LSTORE = 6,   // local sort, write-out
+  PF_C_FILL = 7,     // fill items
+  PF_P_GRAB = 8,     // producer: taking work from the queue
+  PF_P_EMPTY = 9,    // producer: waiting for a free stage
+  PF_P_LEMPTY = 10,  // producer: waiting for the tile region
+  PF_P_IDLE = 11,    // producer: no work available
+  PF_Q_BUSY = 12,    // completer: finishing jobs
+  PF_Q_IDLE = 13,    // completer: idle
+  PF_N_LOCAL = 14,   // local jobs
+  PF_C_TOTAL = 15,   // consumer leader: whole run
+  PF_P_ISSUE = 16,   // producer: staging (descriptor + bulk copy issue)
+  PF_N_GRAB = 17,    // producer: global queue operations
+  PF_N_LCTA = 18,    // local sort: CTA-wide partitions
+  PF_N_LWARP = 19,   // local sort: warp partitions
+  PF_N_LBIT = 20,    // local sort: register sorts
+  PF_N_ITEMS = 21,   // ring items consumed
+  PF_COUNT = 22
+};
+#ifdef GQS_PROFILE
+#define GQS_PROF_DECL unsigned long long prof_[PF_COUNT] = {};
+#define GQS_PROF_T(v) const long long v = clock64();
+#define GQS_PROF_ADD(i, v) prof_[i] += (unsigned long long)(clock64() - (v));
+#define GQS_PROF_CNT(i, n) prof_[i] += (unsigned long long)(n);
+#define GQS_PROF_FLUSH(q)                                             \
+  for (int i_ = 0; i_ < PF_COUNT; ++i_)                               \
+    if (prof_[i_]) atomicAdd(&(q)->prof[i_], prof_[i_]);
+#else
+#define GQS_PROF_DECL
+#define GQS_PROF_T(v)
+#define GQS_PROF_ADD(i, v)
+#define GQS_PROF_CNT(i, n)
+#define GQS_PROF_FLUSH(q)
+#endif
 
 template <class T>
 struct KeyOps;
@@ -91,8 +138,9 @@ struct SortArgs {
   typename KeyOps<T>::B* dn;
   Job* jobs;
   Queue* q;
-  uint32_t capacity;
-  uint32_t epoch;
+  unsigned long long* tmap;  // ticket -> job slot ring (zeroed before each sort)
+  uint32_t capacity;         // job records
+  uint32_t tmask;            // ticket ring size - 1 (a power of two)
   unsigned long long timeout_ns;
 };
 
@@ -118,7 +166,7 @@ struct Cfg {
   static constexpr int TILE_ELEMS = TILE + 2 * E16;
   static constexpr int FILL_INLINE = 16384;  // pivot runs up to this many keys are written by the completer
   static constexpr int FILL_CHUNK = 32768;   // longer runs become queued fill jobs of this grain
-  static constexpr int CQ = 64;              // completer queue slots
+  static constexpr int CQ = 128;             // completer queue slots
   static constexpr int WLIST = 512;          // segments handed from the CTA phase to the warp phase
   static constexpr int CSTACK = 48;          // CTA-phase stack (smaller child first: depth <= log2 TILE + 1)
   static constexpr int WSTACK = 24;          // per-warp stack (same bound for WARP_MAX)
@@ -163,8 +211,8 @@ __device__ __forceinline__ void set_error(Queue* q, uint32_t code, unsigned long
 }
 
 __device__ __forceinline__ unsigned long long progress_word(Queue* q) {
-  return ld_relaxed(&q->done) + ((unsigned long long)ld_relaxed(&q->tail) << 40) +
-         ((unsigned long long)ld_relaxed(&q->head) << 20);
+  return ld_relaxed(&q->done) + ld_relaxed(&q->alloc) * 0x9E3779B97F4A7C15ull +
+         ((unsigned long long)ld_relaxed(&q->grab) << 40);
 }
 
 // A wait that gives up (and records a timeout) only when the whole sort has made no
@@ -247,17 +295,14 @@ __device__ __forceinline__ K kmax() {
 // ---------------------------------------------------------------------------
 // Queue operations.
 
+// Publishes one job; called by all 32 lanes of a warp with the same arguments. Lane 0 writes
+// the record, then every lane writes a share of its ticket-map entries.
 template <class C>
 __device__ bool push_job(const SortArgs<typename C::T>& a, uint32_t kind, uint32_t dir,
                          unsigned long long start, unsigned long long end, unsigned long long pivot,
                          uint32_t depth) {
   using B = typename C::B;
-  const uint32_t slot = atomicAdd(&a.q->tail, 1u);
-  if (slot >= a.capacity) {
-    set_error(a.q, ST_CAPACITY, slot);
-    return false;
-  }
-  Job* j = a.jobs + slot;
+  const int lane = threadIdx.x & 31;
   long long grid = (long long)start;
   uint32_t nch = 1;
   if (kind == JOB_PART) {
@@ -268,20 +313,43 @@ __device__ bool push_job(const SortArgs<typename C::T>& a, uint32_t kind, uint32
     grid -= (long long)((reinterpret_cast<uintptr_t>(a.d + start) & 15u) / sizeof(B));
     nch = (uint32_t)(((long long)end - grid + C::FILL_CHUNK - 1) / C::FILL_CHUNK);
   }
-  j->start = start;
-  j->end = end;
-  j->sstart = start;
-  j->send = end;
-  j->pivot = pivot;
-  j->grid = grid;
-  j->kind = kind;
-  j->dir = dir;
-  j->nchunks = nch;
-  j->cursor = 0;
-  j->remaining = nch;
-  j->depth = depth;
-  __threadfence();
-  st_release(&j->ready, a.epoch);
+  unsigned long long old = 0;
+  uint32_t ok = 1;
+  if (lane == 0) {
+    old = atomicAdd(&a.q->alloc, (1ull << 32) | (unsigned long long)nch);
+    const uint32_t slot = (uint32_t)(old >> 32), t0 = (uint32_t)old;
+    // the ring must still hold every ticket not yet taken once these are added (producers
+    // may hold tickets ahead of the last one created, so `grab` can exceed t0 + nch)
+    const long long untaken = (long long)t0 + (long long)nch - (long long)ld_relaxed(&a.q->grab);
+    if (slot >= a.capacity || untaken > (long long)a.tmask + 1) {
+      set_error(a.q, ST_CAPACITY, slot);
+      ok = 0;
+    } else {
+      Job* j = a.jobs + slot;
+      j->start = start;
+      j->end = end;
+      j->sstart = start;
+      j->send = end;
+      j->pivot = pivot;
+      j->grid = grid;
+      j->kind = kind;
+      j->dir = dir;
+      j->nchunks = nch;
+      j->t0 = t0;
+      j->remaining = nch;
+      j->depth = depth;
+    }
+  }
+  ok = __shfl_sync(0xffffffffu, ok, 0);
+  old = __shfl_sync(0xffffffffu, old, 0);
+  if (!ok) return false;
+  __syncwarp();
+  __threadfence();  // the record (written by lane 0, ordered by the warp barrier) before its tickets
+  const uint32_t slot = (uint32_t)(old >> 32), t0 = (uint32_t)old;
+  for (uint32_t i = lane; i < nch; i += 32) {
+    const uint32_t t = t0 + i;
+    st_relaxed(a.tmap + (t & a.tmask), ((unsigned long long)(t + 1) << 32) | slot);
+  }
   return true;
 }
 
@@ -341,11 +409,11 @@ __device__ unsigned long long dispatch_range(const SortArgs<typename C::T>& a, u
     return m;
   }
   if (m <= (unsigned long long)C::TILE) {
-    if (lane == 0) push_job<C>(a, JOB_LOCAL, dir, s, e, 0, depth);
+    push_job<C>(a, JOB_LOCAL, dir, s, e, 0, depth);
     return 0;
   }
   const B pv = sample_pivot_global<C, 4>(src, s, m);
-  if (lane == 0) push_job<C>(a, JOB_PART, dir, s, e, (unsigned long long)pv, depth);
+  push_job<C>(a, JOB_PART, dir, s, e, (unsigned long long)pv, depth);
   return 0;
 }
 
@@ -383,32 +451,35 @@ struct Persistent {
   using Ops = typename C::Ops;
 
   static __device__ __forceinline__ void cbar() { named_bar_sync(1, C::NC); }
+  static __device__ __forceinline__ bool tid0_of_cta() { return threadIdx.x == 0; }
 
   // ---- producer ---------------------------------------------------------
-  // Take one chunk of the oldest job that still has chunks. Returns ITEM_NONE when the queue
-  // is momentarily empty, ITEM_TERM when every key is placed or the sort has failed.
-  static __device__ uint32_t grab(const SortArgs<T>& a, uint32_t& slot, uint32_t& chunk) {
-    for (;;) {
-      if (ld_relaxed(&a.q->error)) return ITEM_TERM;
-      const uint32_t h = ld_relaxed(&a.q->head);
-      const uint32_t t = ld_relaxed(&a.q->tail);
-      if (h < t) {
-        if (h >= a.capacity) return ITEM_TERM;
-        Job* j = a.jobs + h;
-        if (ld_acquire(&j->ready) != a.epoch) return ITEM_NONE;  // allocated, not yet published
-        const uint32_t nch = __ldcg(&j->nchunks);
-        const uint32_t c = atomicAdd(&j->cursor, 1u);
-        if (c < nch) {
-          slot = h;
-          chunk = c;
-          return __ldcg(&j->kind);
-        }
-        atomicCAS(&a.q->head, h, h + 1);
-        continue;
-      }
-      if (ld_relaxed(&a.q->done) >= ld_relaxed(&a.q->total)) return ITEM_TERM;
-      return ITEM_NONE;
-    }
+  // Work is taken by ticket: one atomic on the queue's grab counter reserves kTake consecutive
+  // tickets, and lanes 0..kTake-1 resolve them through the ticket map in parallel. Each ticket
+  // is one chunk of one job, so no two producers ever contend for the same chunk.
+  static constexpr uint32_t kTake = 4;
+
+  struct Ticket {
+    unsigned long long js, je, pivot;
+    long long grid;
+    uint32_t slot, kind, dir, chunk;
+  };
+
+  // Resolves this lane's ticket if it is published; returns whether it is.
+  static __device__ __forceinline__ bool resolve(const SortArgs<T>& a, uint32_t t, Ticket& tk) {
+    const unsigned long long e = ld_acquire(a.tmap + (t & a.tmask));
+    if ((uint32_t)(e >> 32) != t + 1u) return false;
+    const uint32_t slot = (uint32_t)e;
+    const Job* j = a.jobs + slot;
+    tk.slot = slot;
+    tk.kind = __ldcg(&j->kind);
+    tk.dir = __ldcg(&j->dir);
+    tk.js = __ldcg(&j->start);
+    tk.je = __ldcg(&j->end);
+    tk.pivot = __ldcg(&j->pivot);
+    tk.grid = __ldcg(&j->grid);
+    tk.chunk = t - __ldcg(&j->t0);
+    return true;
   }
 
   // Stage src[cs, ce) into shared memory at `dst`, rounded out to whole 16-byte granules of
@@ -428,17 +499,43 @@ struct Persistent {
 
   static __device__ void producer(const SortArgs<T>& a, Smem<C>& sm) {
     const int lane = threadIdx.x & 31;
-    uint32_t k = 0, nloc = 0;
+    GQS_PROF_DECL
+    uint32_t k = 0, nloc = 0, nops = 0;
     bool need_flush = false;  // partition chunks were handed out since the last drain
     uint32_t failed = 0;
     Waiter idle(a.q);
     bool idling = false;
+    uint32_t tb = 0, next = kTake, resolved = 0;
+    Ticket mine;
+    mine.slot = 0;
     for (;;) {
-      uint32_t kind = ITEM_NONE, slot = 0, chunk = 0;
-      if (lane == 0) {
-        kind = grab(a, slot, chunk);
-        if (kind == ITEM_NONE) {
-          if (need_flush) {
+      GQS_PROF_T(t0)
+      if (next == kTake) {  // take the next batch of tickets
+        uint32_t b = 0;
+        if (lane == 0) b = atomicAdd(&a.q->grab, kTake);
+        tb = __shfl_sync(0xffffffffu, b, 0);
+        next = 0;
+        resolved = 0;
+        ++nops;
+      }
+      if (!((resolved >> next) & 1u)) {
+        bool ok = false;
+        if (lane < (int)kTake && !((resolved >> lane) & 1u)) ok = resolve(a, tb + lane, mine);
+        resolved |= __ballot_sync(0xffffffffu, ok);
+      }
+      GQS_PROF_ADD(PF_P_GRAB, t0)
+      uint32_t kind;
+      if ((resolved >> next) & 1u) {
+        kind = __shfl_sync(0xffffffffu, mine.kind, next);  // job kinds double as item kinds
+        idling = false;
+      } else {
+        // The next ticket is not published yet: more work is coming, or the sort is over.
+        kind = ITEM_NONE;
+        if (lane == 0) {
+          GQS_PROF_T(t1)
+          if (ld_relaxed(&a.q->error) || ld_relaxed(&a.q->done) >= ld_relaxed(&a.q->total)) {
+            kind = ITEM_TERM;
+          } else if (need_flush) {
             kind = ITEM_FLUSH;  // let the consumers finish what they hold before idling
           } else {
             if (!idling) {
@@ -447,33 +544,42 @@ struct Persistent {
             }
             if (!idle.step(a.q, a.timeout_ns, 1, true)) kind = ITEM_TERM;
           }
-        } else {
-          idling = false;
+          GQS_PROF_ADD(PF_P_IDLE, t1)
         }
+        kind = __shfl_sync(0xffffffffu, kind, 0);
+        if (kind == ITEM_NONE) continue;
       }
-      kind = __shfl_sync(0xffffffffu, kind, 0);
-      if (kind == ITEM_NONE) continue;
+      const bool real = kind == ITEM_PART || kind == ITEM_LOCAL || kind == ITEM_FILL;
+      const uint32_t src_lane = real ? next : 0u;
+      const uint32_t slot = __shfl_sync(0xffffffffu, mine.slot, src_lane);
+      const uint32_t dir = __shfl_sync(0xffffffffu, mine.dir, src_lane);
+      const uint32_t chunk = __shfl_sync(0xffffffffu, mine.chunk, src_lane);
+      const unsigned long long js = __shfl_sync(0xffffffffu, mine.js, src_lane);
+      const unsigned long long je = __shfl_sync(0xffffffffu, mine.je, src_lane);
+      const unsigned long long pivot = __shfl_sync(0xffffffffu, mine.pivot, src_lane);
+      const long long grid = __shfl_sync(0xffffffffu, mine.grid, src_lane);
       const uint32_t s = k % C::STAGES;
       if (lane == 0) {
-        if (!mbar_wait(&sm.empty[s], ((k / C::STAGES) & 1u) ^ 1u, a.q, a.timeout_ns, 2)) {
+        GQS_PROF_T(t2)
+        const bool got = mbar_wait(&sm.empty[s], ((k / C::STAGES) & 1u) ^ 1u, a.q, a.timeout_ns, 2);
+        GQS_PROF_ADD(PF_P_EMPTY, t2)
+        GQS_PROF_T(t3)
+        if (!got) {
           failed = 1;
-        } else if (kind == ITEM_TERM || kind == ITEM_FLUSH) {
+        } else if (!real) {
           sm.desc[s].kind = kind;
           mbar_arrive(&sm.full[s]);
           need_flush = false;
         } else {
-          const Job* j = a.jobs + slot;
-          const unsigned long long js = __ldcg(&j->start), je = __ldcg(&j->end);
-          const uint32_t dir = __ldcg(&j->dir);
           Desc& dd = sm.desc[s];
           dd.kind = kind;
           dd.job = slot;
           dd.dir = dir;
-          dd.pivot = __ldcg(&j->pivot);
+          dd.pivot = pivot;
           const B* src = dir ? a.d : a.dn;
           if (kind == ITEM_PART || kind == ITEM_FILL) {
             const long long grain = kind == ITEM_PART ? C::CHUNK : C::FILL_CHUNK;
-            const long long g0 = __ldcg(&j->grid) + (long long)chunk * grain;
+            const long long g0 = grid + (long long)chunk * grain;
             const unsigned long long cs = (long long)js > g0 ? js : (unsigned long long)g0;
             const unsigned long long ce0 = (unsigned long long)(g0 + grain);
             const unsigned long long ce = ce0 < je ? ce0 : je;
@@ -488,7 +594,10 @@ struct Persistent {
               need_flush = false;
             }
           } else {  // ITEM_LOCAL: the tile region is single-buffered
-            if (!mbar_wait(&sm.lempty, (nloc & 1u) ^ 1u, a.q, a.timeout_ns, 3)) {
+            GQS_PROF_T(t4)
+            const bool free_tile = mbar_wait(&sm.lempty, (nloc & 1u) ^ 1u, a.q, a.timeout_ns, 3);
+            GQS_PROF_ADD(PF_P_LEMPTY, t4)
+            if (!free_tile) {
               failed = 1;
             } else {
               dd.gbeg = js;
@@ -500,10 +609,12 @@ struct Persistent {
             }
           }
         }
+        GQS_PROF_ADD(PF_P_ISSUE, t3)
       }
       failed = __shfl_sync(0xffffffffu, failed, 0);
       if (failed) break;
       ++k;
+      if (real) ++next;
       if (kind == ITEM_TERM) break;
     }
     if (failed && lane == 0) {
@@ -515,6 +626,10 @@ struct Persistent {
       }
       if (nloc) mbar_wait(&sm.lfull, (nloc - 1) & 1u, a.q, 200000000ull, 9);
       sts_release(&sm.term, 2u);
+    }
+    if (lane == 0) {
+      GQS_PROF_CNT(PF_N_GRAB, nops)
+      GQS_PROF_FLUSH(a.q)
     }
   }
 
@@ -538,7 +653,7 @@ struct Persistent {
         for (unsigned long long i = ss + lane; i < se; i += 32) a.d[i] = raw;
         placed += plen;
         st_fill += plen;
-      } else if (lane == 0) {
+      } else {
         push_job<C>(a, JOB_FILL, 0u, ss, se, (unsigned long long)pv, depth);
       }
     }
@@ -550,21 +665,24 @@ struct Persistent {
     if (depth + 1 > st_depth) st_depth = depth + 1;
   }
 
+  // The completer takes up to 32 posted chunks at once; each lane retires one with an
+  // acquire-release decrement of its job's chunk count, and the warp finishes every job
+  // whose count reached zero.
   static __device__ void completer(const SortArgs<T>& a, Smem<C>& sm) {
     const int lane = threadIdx.x & 31;
+    GQS_PROF_DECL
     unsigned long long st_tiny = 0, st_fill = 0;
     uint32_t st_depth = 0, st_jobs = 0;
     uint32_t head = 0;
     Waiter w(a.q);
     bool idling = false;
     for (;;) {
-      uint32_t slot = 0, state = 0;  // 0 none, 1 item, 2 exit
+      uint32_t navail = 0, state = 0;  // state: 0 none, 1 items, 2 exit
+      GQS_PROF_T(tq)
       if (lane == 0) {
         const uint32_t t = lds_acquire(&sm.cq_tail);
         if (t != head) {
-          slot = sm.cq[head % C::CQ];
-          ++head;
-          sts_release(&sm.cq_head, head);
+          navail = min(t - head, 32u);
           state = 1;
           idling = false;
         } else if (lds_acquire(&sm.term)) {
@@ -579,21 +697,34 @@ struct Persistent {
       }
       state = __shfl_sync(0xffffffffu, state, 0);
       if (state == 2) break;
-      if (state == 0) continue;
-      slot = __shfl_sync(0xffffffffu, slot, 0);
-      uint32_t old = 0;
-      if (lane == 0) {
-        __threadfence();
-        old = atomicSub(&a.jobs[slot].remaining, 1u);
-        __threadfence();
+      if (state == 0) {
+        GQS_PROF_ADD(PF_Q_IDLE, tq)
+        continue;
       }
-      old = __shfl_sync(0xffffffffu, old, 0);
-      if (old == 1u) {
-        complete_job(a, slot, st_tiny, st_fill, st_depth);
+      GQS_PROF_T(tb)
+      navail = __shfl_sync(0xffffffffu, navail, 0);
+      __syncwarp();
+      uint32_t slot = 0, old = 0;
+      if ((uint32_t)lane < navail) {
+        slot = sm.cq[(head + lane) % C::CQ];
+        old = atom_add_acq_rel(&a.jobs[slot].remaining, 0xffffffffu);
+      }
+      head += navail;
+      __syncwarp();
+      if (lane == 0) sts_release(&sm.cq_head, head);
+      uint32_t last = __ballot_sync(0xffffffffu, (uint32_t)lane < navail && old == 1u);
+      while (last) {
+        const int l = __ffs(last) - 1;
+        last &= last - 1;
+        const uint32_t js = __shfl_sync(0xffffffffu, slot, l);
+        __threadfence();
+        complete_job(a, js, st_tiny, st_fill, st_depth);
         ++st_jobs;
       }
+      GQS_PROF_ADD(PF_Q_BUSY, tb)
     }
     if (lane == 0) {
+      GQS_PROF_FLUSH(a.q)
       if (st_tiny) atomicAdd(&a.q->tiny_keys, st_tiny);
       if (st_fill) atomicAdd(&a.q->fill_keys, st_fill);
       if (st_jobs) atomicAdd(&a.q->part_jobs, st_jobs);
@@ -704,7 +835,7 @@ struct Persistent {
 
   // Warp phase: quicksort of one segment in shared memory with an explicit stack
   // (lqsort_kernel's work stack, QuicksortKernels.cl:280-420, run by one warp).
-  static __device__ void warp_quicksort(Smem<C>& sm, B* A, Seg seg, Seg* stk, Queue* q) {
+  static __device__ void warp_quicksort(Smem<C>& sm, B* A, Seg seg, Seg* stk, Queue* q, unsigned long long* lp) {
     const int lane = threadIdx.x & 31;
     const uint32_t ltm = lanemask_lt();
     int sp = 0;
@@ -720,8 +851,14 @@ struct Persistent {
       const uint32_t n = g.e - g.s;
       if (n <= (uint32_t)C::TINY) {
         warp_sort_smem(X, A, g.s, n);
+#ifdef GQS_PROFILE
+        if (tid0_of_cta()) lp[4] += 1;
+#endif
         continue;
       }
+#ifdef GQS_PROFILE
+      if (tid0_of_cta()) lp[3] += 1;
+#endif
       const B p = sample32_smem(X, g.s, n);
       uint32_t lpos = g.s, gpos = g.e;
       for (uint32_t base = g.s; base < g.e; base += 32) {
@@ -763,8 +900,13 @@ struct Persistent {
 
   // CTA-wide local sort of A[0, m) (keys already mapped to comparison keys). On return A
   // holds the sorted keys. (lqsort_kernel, QuicksortKernels.cl:267-421.)
-  static __device__ void local_sort(const SortArgs<T>& a, Smem<C>& sm, B* A, uint32_t m) {
+  // lp (profile builds): {CTA-phase cycles, warp-phase cycles, CTA partitions, warp partitions,
+  // register sorts}; the leader thread's view.
+  static __device__ void local_sort(const SortArgs<T>& a, Smem<C>& sm, B* A, uint32_t m, unsigned long long* lp) {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+#ifdef GQS_PROFILE
+    const long long t_cta = clock64();
+#endif
     const uint32_t ltm = lanemask_lt();
     if (tid == 0) {
       sm.csp = 0;
@@ -791,6 +933,9 @@ struct Persistent {
         cbar();
         continue;
       }
+#ifdef GQS_PROFILE
+      lp[2] += 1;
+#endif
       if (warp == 0) {
         const B pv = sample32_smem(X, g.s, n);
         if (lane == 0) sm.pivot_bc = (unsigned long long)pv;
@@ -851,15 +996,22 @@ struct Persistent {
       cbar();
     }
     // warp phase
+#ifdef GQS_PROFILE
+    const long long t_warp = clock64();
+    lp[0] += (unsigned long long)(t_warp - t_cta);
+#endif
     const int nwl = sm.wl_n;
     for (;;) {
       int idx = 0;
       if (lane == 0) idx = atomicAdd(&sm.wl_next, 1);
       idx = __shfl_sync(0xffffffffu, idx, 0);
       if (idx >= nwl) break;
-      warp_quicksort(sm, A, sm.wlist[idx], sm.wstack[warp], a.q);
+      warp_quicksort(sm, A, sm.wlist[idx], sm.wstack[warp], a.q, lp);
     }
     cbar();
+#ifdef GQS_PROFILE
+    lp[1] += (unsigned long long)(clock64() - t_warp);
+#endif
   }
 
   // Leader-only bounded wait for ring slot k; every consumer reads the verdict after the
@@ -881,11 +1033,15 @@ struct Persistent {
     unsigned long long pend_lb = 0, pend_gb = 0;  // leader only
     unsigned long long st_part = 0, st_local = 0, st_chunks = 0;
     uint32_t st_local_jobs = 0, st_fill_jobs = 0;
+    GQS_PROF_DECL
+    GQS_PROF_T(t_all)
 
     if (tid == 0) leader_wait_slot(a, sm, 0);
     cbar();
     for (;;) {
       if (!sm.cons_ok) break;
+      GQS_PROF_T(t_it)
+      GQS_PROF_CNT(PF_N_ITEMS, 1)
       const uint32_t s = k % C::STAGES;
       (void)mbar_test(&sm.full[s], (k / C::STAGES) & 1u);  // completed; gives this thread acquire order
       const Desc dd = sm.desc[s];
@@ -929,7 +1085,9 @@ struct Persistent {
           Job* j = a.jobs + dd.job;
           new_lb = atomicAdd(&j->sstart, (unsigned long long)ls);
           new_gb = atomicAdd(&j->send, (unsigned long long)(-(long long)gs)) - gs;
+          GQS_PROF_T(tw)
           leader_wait_slot(a, sm, k + 1);
+          GQS_PROF_ADD(PF_C_WAIT, tw)
         }
         cbar();  // #2: bases of the pending chunk published; next slot verdict published
         have_scat = false;
@@ -953,6 +1111,7 @@ struct Persistent {
         ++st_chunks;
         ++npart;
         ++k;
+        GQS_PROF_ADD(PF_C_PART, t_it)
         continue;
       }
 
@@ -976,19 +1135,25 @@ struct Persistent {
       }
       have_pend = false;
       have_scat = false;
+      GQS_PROF_ADD(PF_C_DRAIN, t_it)
 
       if (dd.kind == ITEM_TERM) break;
       if (dd.kind == ITEM_FILL) {
         // Queued pivot-run fill: write the raw pivot over d[gbeg, gbeg + len).
+        GQS_PROF_T(tf)
         const B raw = Ops::raw((B)dd.pivot);
         B* out = a.d + dd.gbeg;
         for (uint32_t i = tid; i < dd.len; i += C::NC) out[i] = raw;
         ++st_fill_jobs;
+        GQS_PROF_ADD(PF_C_FILL, tf)
         if (tid == 0) atomicAdd(&a.q->done, (unsigned long long)dd.len);
       } else if (dd.kind == ITEM_LOCAL) {
+        GQS_PROF_T(tl)
         if (tid == 0) sm.lok = mbar_wait(&sm.lfull, nloc & 1u, a.q, a.timeout_ns, 7) ? 1u : 0u;
         cbar();
         if (!sm.lok) break;
+        GQS_PROF_ADD(PF_C_LWAIT, tl)
+
         (void)mbar_test(&sm.lfull, nloc & 1u);
         B* A = sm.tileA + dd.off;
         const uint32_t m = dd.len;
@@ -996,7 +1161,16 @@ struct Persistent {
           for (uint32_t i = tid; i < m; i += C::NC) A[i] = Ops::key(A[i]);
           cbar();
         }
-        local_sort(a, sm, A, m);
+        unsigned long long lp[5] = {0, 0, 0, 0, 0};
+        local_sort(a, sm, A, m, lp);
+        GQS_PROF_CNT(PF_C_LCTA, lp[0])
+        GQS_PROF_CNT(PF_C_LWARP, lp[1])
+        GQS_PROF_CNT(PF_N_LCTA, lp[2])
+        GQS_PROF_CNT(PF_N_LWARP, lp[3])
+        GQS_PROF_CNT(PF_N_LBIT, lp[4])
+        GQS_PROF_CNT(PF_N_LOCAL, 1)
+        GQS_PROF_T(ts)
+
         if (!Ops::kIdentity) {
           for (uint32_t i = tid; i < m; i += C::NC) A[i] = Ops::raw(A[i]);
         }
@@ -1028,6 +1202,7 @@ struct Persistent {
           mbar_arrive(&sm.lempty);
           atomicAdd(&a.q->done, (unsigned long long)m);
         }
+        GQS_PROF_ADD(PF_C_LSTORE, ts)
         st_local += m;
         ++st_local_jobs;
         ++nloc;
@@ -1037,7 +1212,9 @@ struct Persistent {
       cbar();
       ++k;
     }
+    GQS_PROF_ADD(PF_C_TOTAL, t_all)
     if (tid == 0) {
+      GQS_PROF_FLUSH(a.q)
       bulk_wait_all();
       sts_release(&sm.term, 1u);
       if (st_part) atomicAdd(&a.q->part_keys, st_part);

@@ -29,8 +29,9 @@ struct LaunchParams {
   void* dn;
   Job* jobs;
   Queue* q;
+  unsigned long long* tmap;  // ticket ring, zeroed before the sort
   uint32_t capacity;
-  uint32_t epoch;
+  uint32_t tmask;
   unsigned long long timeout_ns;
   const unsigned long long* offsets;  // nseg + 1 device offsets, or null for one segment [0, n)
   unsigned long long n;               // keys when offsets is null

@@ -38,8 +38,9 @@ struct VariantOps {
     a.dn = static_cast<B*>(p.dn);
     a.jobs = p.jobs;
     a.q = p.q;
+    a.tmap = p.tmap;
     a.capacity = p.capacity;
-    a.epoch = p.epoch;
+    a.tmask = p.tmask;
     a.timeout_ns = p.timeout_ns;
     const uint32_t nseg = p.offsets ? p.nseg : 1u;
     const uint32_t seed_blocks = (nseg + 7u) / 8u;  // 8 warps per 256-thread block, one per segment

@@ -30,7 +30,7 @@ EXPORTS = [
     "gqs_sort_u32_dev", "gqs_sort_f32_dev", "gqs_sort_f64_dev",
     "gqs_sort_segments_u32_dev", "gqs_sort_segments_f32_dev", "gqs_sort_segments_f64_dev",
     "gqs_sort_segments_u32", "gqs_sort_segments_f32", "gqs_sort_segments_f64",
-    "gqs_sync", "gqs_last_stats", "gqs_variant_count", "gqs_variant_describe", "gqs_set_variant",
+    "gqs_sync", "gqs_last_stats", "gqs_last_profile", "gqs_variant_count", "gqs_variant_describe", "gqs_set_variant",
     "gqs_get_variant", "gqs_strerror", "gqs_version",
 ]
 
@@ -72,7 +72,7 @@ def load_library(path: str | None = None) -> C.CDLL:
     global _lib
     if _lib is not None and path is None:
         return _lib
-    p = path or LIB_PATH
+    p = path or os.environ.get("GQS_LIB") or LIB_PATH
     if not os.path.exists(p):
         raise FileNotFoundError(f"{p} is missing: build it with __graft_entry__.build() "
                                 "(the sort has no CPU fallback)")
@@ -103,6 +103,8 @@ def load_library(path: str | None = None) -> C.CDLL:
     lib.gqs_sync.restype = st
     lib.gqs_last_stats.argtypes = [vp, C.POINTER(Stats)]
     lib.gqs_last_stats.restype = st
+    lib.gqs_last_profile.argtypes = [vp, C.POINTER(C.c_uint64), sz]
+    lib.gqs_last_profile.restype = C.c_int
     lib.gqs_variant_count.argtypes = [C.c_int]
     lib.gqs_variant_count.restype = C.c_int
     lib.gqs_variant_describe.argtypes = [C.c_int, C.c_int, C.POINTER(VariantDesc)]
@@ -196,6 +198,15 @@ class Context:
         d = s.as_dict()
         d["call_status"] = code
         return d
+
+    PROFILE_SLOTS = ["c_wait", "c_part", "c_drain", "c_lwait", "c_lcta", "c_lwarp", "c_lstore", "c_fill",
+                     "p_grab", "p_empty", "p_lempty", "p_idle", "q_busy", "q_idle", "n_local", "c_total",
+                     "p_issue", "n_grab", "n_lcta", "n_lwarp", "n_lbit", "n_items"]
+
+    def profile(self) -> dict:
+        buf = (C.c_uint64 * 32)()
+        k = self.lib.gqs_last_profile(self.h, buf, 32)
+        return {name: int(buf[i]) for i, name in enumerate(self.PROFILE_SLOTS) if i < k}
 
     def set_variant(self, dtype: str, v: int) -> None:
         _check(self.lib.gqs_set_variant(self.h, DTYPES[dtype], v), "gqs_set_variant")

@@ -124,6 +124,10 @@ gqs_status gqs_sync(gqs_ctx* ctx);
 /* Statistics of the last completed sort (waits for it if it is still running). */
 gqs_status gqs_last_stats(gqs_ctx* ctx, gqs_stats* out);
 
+/* Per-role cycle counters of the last sort, filled only by a library built with -DGQS_PROFILE
+ * (zeros otherwise). Writes up to n values and returns the number written. */
+int gqs_last_profile(gqs_ctx* ctx, uint64_t* out, size_t n);
+
 /* Kernel variants available for a key type, and the one the context currently uses. */
 int gqs_variant_count(int dtype);
 gqs_status gqs_variant_describe(int dtype, int variant, gqs_variant_desc* out);
