@@ -44,7 +44,7 @@ def parse():
     p.add_argument("--steps", type=int, default=5)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--config", default="plain", choices=["plain", "batched"])
+    p.add_argument("--config", default="plain", choices=["plain", "batched", "tiles"])
     p.add_argument("--dtype", default="u32", choices=["u32", "f32", "f64"])
     p.add_argument("--dist", default="uniform")
     p.add_argument("--log2n", type=int, default=28)
@@ -66,6 +66,8 @@ def dist_env():
 def workload_name(args, n):
     if args.config == "batched":
         return f"batched segmented sort: 4096 uint32 arrays, lengths log-uniform in [32, 2^20], {n} keys"
+    if args.config == "tiles":
+        return f"segmented sort of 8000-key {args.dtype} arrays (on-chip sort only), {n} keys"
     return f"plain sort, 2^{args.log2n} {args.dtype} keys, {args.dist}"
 
 
@@ -200,7 +202,7 @@ def main():
     if args.impl == "reference":
         run_reference(args)
         return
-    if args.profile:
+    if args.profile and not os.environ.get("GQS_LIB"):
         import build_lib
         os.environ["GQS_LIB"] = build_lib.build(profile=True)["lib"]
     import torch
@@ -224,15 +226,21 @@ def main():
 
     # ---- input
     offsets = None
+    nseg = 4096
     if args.config == "batched":
-        off = gqs_ctypes.segment_offsets(SEED + rank, 4096, 32, 1 << 20)
+        off = gqs_ctypes.segment_offsets(SEED + rank, nseg, 32, 1 << 20)
         n = int(off[-1])
         offsets = torch.from_numpy(off.astype(np.int64)).cuda()
+    elif args.config == "tiles":
+        nseg = (1 << args.log2n) // 8000
+        off = np.arange(nseg + 1, dtype=np.int64) * (6000 if args.dtype == "f64" else 8000)
+        n = int(off[-1])
+        offsets = torch.from_numpy(off).cuda()
     else:
         n = 1 << args.log2n
     host_in = torch.empty(n, dtype=tdt, pin_memory=True)
     hv = host_in.numpy().view(npdt) if args.dtype == "u32" else host_in.numpy()
-    gqs_ctypes.generate(args.dtype, args.dist if args.config == "plain" else "uniform", SEED + rank, n, out=hv)
+    gqs_ctypes.generate(args.dtype, args.dist if args.config != "batched" else "uniform", SEED + rank, n, out=hv)
     pristine = host_in.cuda()
     d = torch.empty_like(pristine)
     dn = torch.empty_like(pristine)
@@ -244,7 +252,7 @@ def main():
         if offsets is None:
             rc = ctx.sort_dev(args.dtype, d.data_ptr(), dn.data_ptr(), n, stream.cuda_stream)
         else:
-            rc = ctx.sort_segments_dev(args.dtype, d.data_ptr(), dn.data_ptr(), n, offsets.data_ptr(), 4096,
+            rc = ctx.sort_segments_dev(args.dtype, d.data_ptr(), dn.data_ptr(), n, offsets.data_ptr(), nseg,
                                        stream.cuda_stream)
         if rc != 0:
             raise RuntimeError(f"sort enqueue failed: {gqs_ctypes.STATUS.get(rc, rc)}")
@@ -332,7 +340,7 @@ def main():
     km = float(np.mean(kernel_ms))
     ab = float(np.mean(algo_bytes))
     achieved = ab / (km / 1e3) / 1e9
-    wkey = f"plain_{args.dtype}_{args.dist}_2^{args.log2n}" if offsets is None else "batched_u32_4096"
+    wkey = f"plain_{args.dtype}_{args.dist}_2^{args.log2n}" if offsets is None else f"{args.config}_{args.dtype}"
     traffic = ncu_traffic(wkey)
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": traffic, "kernel": "gqs::persistent_kernel", "kernel_ms": km,

@@ -22,6 +22,7 @@
 // and no float/double compare instruction is issued. Memory always holds the caller's raw bits.
 #pragma once
 #include <cstdint>
+#include <cstring>
 #include "gqs_ptx.cuh"
 
 namespace gqs {
@@ -86,7 +87,14 @@ enum : int {
   PF_N_LWARP = 19,   // local sort: warp partitions
   PF_N_LBIT = 20,    // local sort: register sorts
   PF_N_ITEMS = 21,   // ring items consumed
-  PF_COUNT = 22
+  PF_C_COUNT = 22,   // consumers: load + count of a chunk, up to barrier #1
+  PF_C_LEADER = 23,  // consumers: barrier #1 to barrier #2 (leader's reservation work)
+  PF_C_SCATTER = 24, // consumers: scatter of the pending chunk
+  PF_W_WAIT = 25,    // local sort, summed over warps: cycles inside slices (incl. finishing)
+  PF_W_PART = 26,    // local sort: segments finished
+  PF_W_BIT = 27,     // local sort, summed over warps: register sorts
+  PF_W_SEGS = 28,    // (unused)
+  PF_COUNT = 29
 };
 #ifdef GQS_PROFILE
 #define GQS_PROF_DECL unsigned long long prof_[PF_COUNT] = {};
@@ -153,7 +161,7 @@ struct Cfg {
   using B = typename Ops::B;
   static constexpr int NCW = NCW_;
   static constexpr int NC = NCW * 32;
-  static constexpr int NT = NC + 64;
+  static constexpr int NT = NC + 96;  // + producer, completer and reserver warps
   static constexpr int TILE = TILE_;
   static constexpr int CHUNK = CHUNK_;
   static constexpr int STAGES = STAGES_;
@@ -167,9 +175,12 @@ struct Cfg {
   static constexpr int FILL_INLINE = 16384;  // pivot runs up to this many keys are written by the completer
   static constexpr int FILL_CHUNK = 32768;   // longer runs become queued fill jobs of this grain
   static constexpr int CQ = 128;             // completer queue slots
-  static constexpr int WLIST = 512;          // segments handed from the CTA phase to the warp phase
-  static constexpr int CSTACK = 48;          // CTA-phase stack (smaller child first: depth <= log2 TILE + 1)
-  static constexpr int WSTACK = 24;          // per-warp stack (same bound for WARP_MAX)
+  static constexpr int RQ = 32;              // reservation request slots
+  // Local sort: segments are cut into slices of SLICE_KPL keys per lane (32 * SLICE_KPL per
+  // slice) that any warp may partition; LREC segment records live in shared memory per tile.
+  static constexpr int SLICE_KPL = sizeof(B) == 8 ? 8 : 16;
+  static constexpr int SLICE = 32 * SLICE_KPL;
+  static constexpr int LREC = 4 * TILE / TINY + 64;
   static_assert(CHUNK % NC == 0, "chunk must be a multiple of the consumer threads");
   static_assert((CHUNK * sizeof(B)) % 16 == 0, "chunk must be a multiple of 16 bytes");
   static_assert(TILE > TINY, "tile must exceed the register sort");
@@ -177,6 +188,17 @@ struct Cfg {
 
 struct Seg {
   uint32_t s, e, buf;
+};
+
+// A segment of the on-chip tile being partitioned slice by slice (shared memory).
+struct LRec {
+  unsigned long long pivot;
+  uint32_t s, e, buf, nsl;  // [s, e) of buffer `buf`, cut into nsl slices
+  uint32_t cursor;          // slices taken
+  uint32_t remaining;       // slices not yet scattered
+  uint32_t lt, gt;          // keys reserved below / above the pivot
+  uint32_t seq;             // index + 1 once the record is published
+  uint32_t pad;
 };
 
 struct Desc {
@@ -193,14 +215,15 @@ struct alignas(128) Smem {
   uint64_t full[C::STAGES], empty[C::STAGES], lfull, lempty;
   Desc desc[C::STAGES];
   uint32_t wlt[3][C::NCW], wgt[3][C::NCW];  // per-warp totals: count (k), scatter (k-1), free (k-2)
-  unsigned long long blt[3], bgt[3];
   uint32_t cq[C::CQ];
   uint32_t cq_head, cq_tail, term, cons_ok, lok;
-  int csp, wl_n, wl_next;
-  unsigned long long pivot_bc;
-  Seg cstack[C::CSTACK];
-  Seg wlist[C::WLIST];
-  Seg wstack[C::NCW][C::WSTACK];
+  // output-range reservations: consumer leader -> reserver warp -> consumers
+  uint32_t rq_job[C::RQ], rq_ls[C::RQ], rq_gs[C::RQ], rs_done[C::RQ];
+  unsigned long long rs_lb[C::RQ], rs_gb[C::RQ];
+  uint32_t rq_tail;
+  // local sort: segment records and their queue
+  uint32_t lr_head, lr_tail, ls_done;
+  LRec lrec[C::LREC];
 };
 
 // ---------------------------------------------------------------------------
@@ -252,23 +275,46 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, Queue*
 // ---------------------------------------------------------------------------
 // Warp-level bitonic sort of 32*R keys held R per lane; network element e = lane*R + r.
 // (Replaces the reference's work-group bitonic network, QuicksortKernels.cl:40-68.)
+// Flip form: each merge of size k starts by comparing e with its mirror e ^ (k-1), then
+// half-cleaners compare e with e ^ j; the lower index always keeps the minimum, so no
+// compare-exchange needs a per-element direction.
 template <int R, class K>
 __device__ __forceinline__ void warp_bitonic(K (&v)[R]) {
   const int lane = threadIdx.x & 31;
 #pragma unroll
   for (int k = 2; k <= 32 * R; k <<= 1) {
+    if (k <= R) {
 #pragma unroll
-    for (int j = k >> 1; j > 0; j >>= 1) {
+      for (int r = 0; r < R; ++r) {
+        const int pr = r ^ (k - 1);
+        if (pr > r) {
+          const K a = v[r], b = v[pr];
+          v[r] = a < b ? a : b;
+          v[pr] = a < b ? b : a;
+        }
+      }
+    } else {
+      const int lj = (k - 1) / R;
+      const bool lower = (lane & (k / R / 2)) == 0;
+      K t[R];
+#pragma unroll
+      for (int r = 0; r < R; ++r) t[r] = __shfl_xor_sync(0xffffffffu, v[R - 1 - r], lj);
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        const K a = v[r], b = t[r];
+        v[r] = ((a > b) == lower) ? b : a;
+      }
+    }
+#pragma unroll
+    for (int j = k >> 2; j > 0; j >>= 1) {
       if (j < R) {
 #pragma unroll
         for (int r = 0; r < R; ++r) {
           const int pr = r ^ j;
           if (pr > r) {
-            const bool asc = (((lane * R + r) & k) == 0);
-            K a = v[r], b = v[pr];
-            K lo = a < b ? a : b, hi = a < b ? b : a;
-            v[r] = asc ? lo : hi;
-            v[pr] = asc ? hi : lo;
+            const K a = v[r], b = v[pr];
+            v[r] = a < b ? a : b;
+            v[pr] = a < b ? b : a;
           }
         }
       } else {
@@ -276,11 +322,9 @@ __device__ __forceinline__ void warp_bitonic(K (&v)[R]) {
         const bool lower = (lane & lj) == 0;
 #pragma unroll
         for (int r = 0; r < R; ++r) {
-          const bool asc = (((lane * R + r) & k) == 0);
-          K b = __shfl_xor_sync(0xffffffffu, v[r], lj);
-          K a = v[r];
-          K lo = a < b ? a : b, hi = a < b ? b : a;
-          v[r] = (lower == asc) ? lo : hi;
+          const K a = v[r];
+          const K b = __shfl_xor_sync(0xffffffffu, a, lj);
+          v[r] = ((a > b) == lower) ? b : a;
         }
       }
     }
@@ -369,23 +413,33 @@ __device__ typename C::B sample_pivot_global(const typename C::B* src, unsigned 
   return __shfl_sync(0xffffffffu, v[0], 16);
 }
 
-// One warp sorts src[a, a+m) (m <= TINY) into d[a, a+m).
-template <class C>
-__device__ void warp_sort_global(const typename C::B* src, typename C::B* d, unsigned long long a, uint32_t m) {
+// One warp sorts src[a, a+m) (m <= 32*R) into d[a, a+m) with a network of 32*R keys.
+template <class C, int R>
+__device__ __noinline__ void warp_sort_global_r(const typename C::B* src, typename C::B* d, unsigned long long a,
+                                                uint32_t m) {
   using B = typename C::B;
   const int lane = threadIdx.x & 31;
-  B v[C::R];
+  B v[R];
 #pragma unroll
-  for (int r = 0; r < C::R; ++r) {
-    const uint32_t e = lane * C::R + r;
+  for (int r = 0; r < R; ++r) {
+    const uint32_t e = r * 32 + lane;  // input layout is free; this one coalesces
     v[r] = e < m ? C::Ops::key(__ldcg(src + a + e)) : kmax<B>();
   }
-  warp_bitonic<C::R>(v);
+  warp_bitonic<R>(v);
 #pragma unroll
-  for (int r = 0; r < C::R; ++r) {
-    const uint32_t e = lane * C::R + r;
+  for (int r = 0; r < R; ++r) {
+    const uint32_t e = lane * R + r;
     if (e < m) d[a + e] = C::Ops::raw(v[r]);
   }
+}
+
+// One warp sorts src[a, a+m) (m <= TINY) into d[a, a+m), with the smallest network that fits.
+template <class C>
+__device__ __forceinline__ void warp_sort_global(const typename C::B* src, typename C::B* d, unsigned long long a,
+                                                 uint32_t m) {
+  if (m <= 64u) warp_sort_global_r<C, 2>(src, d, a, m);
+  else if (m <= 128u || C::R <= 4) warp_sort_global_r<C, (C::R < 4 ? C::R : 4)>(src, d, a, m);
+  else warp_sort_global_r<C, C::R>(src, d, a, m);
 }
 
 // Decide what to do with a range whose keys sit in `src` (dir says which buffer that is).
@@ -732,6 +786,64 @@ struct Persistent {
     }
   }
 
+  // ---- reserver ---------------------------------------------------------
+  // Reserves each counted chunk's output ranges in its job (the reference's two atomics on
+  // parent.sstart / parent.send, QuicksortKernels.cl:183-186). Lane l of the warp serves
+  // request next + l, so up to 32 reservations are in flight and no consumer thread ever
+  // waits on a global atomic.
+  static __device__ void reserver(const SortArgs<T>& a, Smem<C>& sm) {
+    const int lane = threadIdx.x & 31;
+    uint32_t next = 0;
+    Waiter w(a.q);
+    bool idling = false;
+    for (;;) {
+      uint32_t n = 0, state = 0;
+      if (lane == 0) {
+        const uint32_t t = lds_acquire(&sm.rq_tail);
+        if (t != next) {
+          n = min(t - next, 32u);
+          state = 1;
+          idling = false;
+        } else if (lds_acquire(&sm.term)) {
+          state = 2;
+        } else {
+          if (!idling) {
+            w = Waiter(a.q);
+            idling = true;
+          }
+          if (!w.step(a.q, a.timeout_ns, 8, true)) state = 2;
+        }
+      }
+      state = __shfl_sync(0xffffffffu, state, 0);
+      if (state == 2) break;
+      if (state == 0) continue;
+      n = __shfl_sync(0xffffffffu, n, 0);
+      __syncwarp();
+      if ((uint32_t)lane < n) {
+        const uint32_t i = next + lane, e = i % C::RQ;
+        Job* j = a.jobs + sm.rq_job[e];
+        const uint32_t ls = sm.rq_ls[e], gs = sm.rq_gs[e];
+        const unsigned long long lb = atomicAdd(&j->sstart, (unsigned long long)ls);
+        const unsigned long long gb = atomicAdd(&j->send, (unsigned long long)(-(long long)gs)) - gs;
+        sm.rs_lb[e] = lb;
+        sm.rs_gb[e] = gb;
+        sts_release(&sm.rs_done[e], i + 1);
+      }
+      next += n;
+    }
+  }
+
+  // Consumer leader: waits (bounded) for reservation `id`; false if the sort has failed.
+  static __device__ __forceinline__ bool leader_wait_reservation(const SortArgs<T>& a, Smem<C>& sm, uint32_t id) {
+    const uint32_t e = id % C::RQ;
+    if (lds_acquire(&sm.rs_done[e]) == id + 1) return true;
+    Waiter w(a.q);
+    while (lds_acquire(&sm.rs_done[e]) != id + 1) {
+      if (!w.step(a.q, a.timeout_ns, 10, false)) return false;
+    }
+    return true;
+  }
+
   // ---- consumers: partition chunks --------------------------------------
   // Post a finished chunk of job `slot` to this CTA's completer.
   static __device__ void post_chunk(const SortArgs<T>& a, Smem<C>& sm, uint32_t slot) {
@@ -747,12 +859,13 @@ struct Persistent {
   }
 
   // Scatter one counted chunk whose keys are in registers: keys below the pivot go to
-  // [lb + warp prefix ...), keys above to [gb + warp prefix ...). Equal keys are dropped; the
-  // completer writes the pivot run. (gqsort_kernel pass 2, QuicksortKernels.cl:190-203.)
-  static __device__ __forceinline__ void scatter_chunk(const B (&keys)[C::KPT], uint32_t len, B p, B* dst,
-                                                       unsigned long long lb, unsigned long long gb,
-                                                       const uint32_t* wlt, const uint32_t* wgt) {
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  // [lb + warp prefix, ...), keys above to [gb + warp prefix, ...). Keys equal to the pivot
+  // (and the pivot-valued padding of a partial chunk) are dropped; the completer writes the
+  // pivot run. (gqsort_kernel pass 2, QuicksortKernels.cl:190-203.)
+  static __device__ __forceinline__ void scatter_chunk(const B (&keys)[C::KPT], B p, B* dst, unsigned long long lb,
+                                                       unsigned long long gb, const uint32_t* wlt,
+                                                       const uint32_t* wgt) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     uint32_t vl = lane < C::NCW ? wlt[lane] : 0u, vg = lane < C::NCW ? wgt[lane] : 0u;
     uint32_t il = vl, ig = vg;
 #pragma unroll
@@ -763,44 +876,62 @@ struct Persistent {
         ig += tg;
       }
     }
-    const unsigned long long lpos0 = lb + (unsigned long long)__shfl_sync(0xffffffffu, il - vl, warp);
-    const unsigned long long gpos0 = gb + (unsigned long long)__shfl_sync(0xffffffffu, ig - vg, warp);
-    unsigned long long lpos = lpos0, gpos = gpos0;
+    B* const lbase = dst + lb + __shfl_sync(0xffffffffu, il - vl, warp);
+    B* const gbase = dst + gb + __shfl_sync(0xffffffffu, ig - vg, warp);
     const uint32_t ltm = lanemask_lt();
+    uint32_t lo = 0, go = 0;
 #pragma unroll
     for (int j = 0; j < C::KPT; ++j) {
-      const uint32_t i = (uint32_t)(j * C::NC + tid);
-      const bool valid = i < len;
       const B kk = Ops::key(keys[j]);
-      const bool isl = valid && kk < p, isg = valid && kk > p;
+      const bool isl = kk < p, isg = kk > p;
       const uint32_t bl = __ballot_sync(0xffffffffu, isl), bg = __ballot_sync(0xffffffffu, isg);
-      if (isl) dst[lpos + __popc(bl & ltm)] = keys[j];
-      if (isg) dst[gpos + __popc(bg & ltm)] = keys[j];
-      lpos += __popc(bl);
-      gpos += __popc(bg);
+      if (isl || isg) {
+        B* const base = isl ? lbase : gbase;
+        const uint32_t o = isl ? lo + __popc(bl & ltm) : go + __popc(bg & ltm);
+        base[o] = keys[j];
+      }
+      lo += __popc(bl);
+      go += __popc(bg);
     }
   }
 
   // ---- consumers: local (on-chip) sort -----------------------------------
+  // lqsort_kernel (QuicksortKernels.cl:267-421) re-done for one CTA. Like the global
+  // partition, every segment of the tile is cut into slices that any consumer warp may take:
+  // the warp counts its slice in registers, reserves output positions at both ends of the
+  // segment with two shared-memory atomics, and scatters into the other buffer. The warp that
+  // scatters a segment's last slice writes its pivot run and publishes the children; children
+  // of at most TINY keys are sorted in registers by that warp at once. No CTA barrier is
+  // needed between levels, so all warps stay busy from the first segment on.
+  // Keys are comparison keys in A (buffer 0) and B (buffer 1); every final key lands in A.
   static __device__ __forceinline__ B* bufp(Smem<C>& sm, B* A, uint32_t buf) { return buf ? sm.tileB : A; }
 
-  // One warp sorts X[s, s+n) (n <= TINY) into A[s, s+n).
-  static __device__ __forceinline__ void warp_sort_smem(const B* X, B* A, uint32_t s, uint32_t n) {
+  // One warp sorts X[s, s+n) (n <= 32*R) into A[s, s+n) with a network of 32*R keys.
+  template <int R>
+  static __device__ __noinline__ void warp_sort_smem_r(const B* X, B* A, uint32_t s, uint32_t n) {
     const int lane = threadIdx.x & 31;
-    B v[C::R];
+    B v[R];
 #pragma unroll
-    for (int r = 0; r < C::R; ++r) {
+    for (int r = 0; r < R; ++r) {
       const uint32_t e = r * 32 + lane;  // any input layout is valid; this one is bank-conflict free
       v[r] = e < n ? X[s + e] : kmax<B>();
     }
     __syncwarp();
-    warp_bitonic<C::R>(v);
+    warp_bitonic<R>(v);
 #pragma unroll
-    for (int r = 0; r < C::R; ++r) {
-      const uint32_t e = lane * C::R + r;
+    for (int r = 0; r < R; ++r) {
+      const uint32_t e = lane * R + r;
       if (e < n) A[s + e] = v[r];
     }
     __syncwarp();
+  }
+
+  // One warp sorts X[s, s+n) (n <= TINY) into A[s, s+n), with the smallest network that fits.
+  static __device__ __forceinline__ void warp_sort_smem(const B* X, B* A, uint32_t s, uint32_t n) {
+    if (n <= 32u) warp_sort_smem_r<1>(X, A, s, n);
+    else if (n <= 64u) warp_sort_smem_r<2>(X, A, s, n);
+    else if (n <= 128u || C::R <= 4) warp_sort_smem_r<(C::R < 4 ? C::R : 4)>(X, A, s, n);
+    else warp_sort_smem_r<C::R>(X, A, s, n);
   }
 
   // Median of 32 evenly spaced samples of X[s, s+n), computed by one warp.
@@ -812,205 +943,193 @@ struct Persistent {
     return __shfl_sync(0xffffffffu, v[0], 16);
   }
 
-  // Place a child segment: singletons go straight to A, small ones to the warp list,
-  // the rest to the CTA stack. Called by one thread.
-  static __device__ __forceinline__ void push_child(Smem<C>& sm, B* A, uint32_t s, uint32_t e, uint32_t buf,
-                                                    Queue* q) {
-    const uint32_t n = e - s;
-    if (n == 0) return;
-    if (n == 1) {
-      if (buf) A[s] = sm.tileB[s];
-      return;
+  // Publishes segment [s, e) of buffer `buf` (longer than TINY) for slicing. Whole warp.
+  static __device__ void lrec_push(const SortArgs<T>& a, Smem<C>& sm, B* A, uint32_t s, uint32_t e,
+                                   uint32_t buf) {
+    const int lane = threadIdx.x & 31;
+    const B p = sample32_smem(bufp(sm, A, buf), s, e - s);
+    if (lane == 0) {
+      const uint32_t idx = atomicAdd(&sm.lr_tail, 1u);
+      if (idx >= (uint32_t)C::LREC) {
+        set_error(a.q, ST_INTERNAL, 0x1EC0ull);
+      } else {
+        LRec& r = sm.lrec[idx];
+        r.pivot = (unsigned long long)p;
+        r.s = s;
+        r.e = e;
+        r.buf = buf;
+        r.nsl = (e - s + C::SLICE - 1) / C::SLICE;
+        r.cursor = 0;
+        r.remaining = r.nsl;
+        r.lt = 0;
+        r.gt = 0;
+        __threadfence_block();
+        *(volatile uint32_t*)&r.seq = idx + 1u;
+      }
     }
-    if (n <= (uint32_t)C::WARP_MAX && sm.wl_n < C::WLIST) {
-      sm.wlist[sm.wl_n++] = Seg{s, e, buf};
-      return;
-    }
-    if (sm.csp < C::CSTACK) {
-      sm.cstack[sm.csp++] = Seg{s, e, buf};
-    } else {
-      set_error(q, ST_INTERNAL, 0xC57ACull);
-    }
+    __syncwarp();
   }
 
-  // Warp phase: quicksort of one segment in shared memory with an explicit stack
-  // (lqsort_kernel's work stack, QuicksortKernels.cl:280-420, run by one warp).
-  static __device__ void warp_quicksort(Smem<C>& sm, B* A, Seg seg, Seg* stk, Queue* q, unsigned long long* lp) {
+  // Places one child of a finished segment: singletons go to A, small children are sorted in
+  // registers now, larger ones become records. Returns the keys it finalised. Whole warp.
+  static __device__ uint32_t place_child(const SortArgs<T>& a, Smem<C>& sm, B* A, uint32_t s, uint32_t e,
+                                         uint32_t buf, unsigned long long* lp) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t n = e - s;
+    if (n <= 1) {
+      if (n == 1 && buf && lane == 0) A[s] = sm.tileB[s];
+      return n;
+    }
+    if (n <= (uint32_t)C::TINY) {
+#ifdef GQS_PROFILE
+      const long long tb0 = clock64();
+#endif
+      warp_sort_smem(bufp(sm, A, buf), A, s, n);
+#ifdef GQS_PROFILE
+      if (lane == 0) lp[7] += (unsigned long long)(clock64() - tb0);
+#endif
+      return n;
+    }
+    lrec_push(a, sm, A, s, e, buf);
+    return 0;
+  }
+
+  // Partitions slice `c` of record `ri` (whole warp); the warp scattering the last slice
+  // finishes the segment.
+  static __device__ void run_slice(const SortArgs<T>& a, Smem<C>& sm, B* A, uint32_t ri, uint32_t c,
+                                   unsigned long long* lp) {
     const int lane = threadIdx.x & 31;
     const uint32_t ltm = lanemask_lt();
-    int sp = 0;
-    if (lane == 0) stk[0] = seg;
-    sp = 1;
-    __syncwarp();
-    while (sp > 0) {
-      const Seg g = stk[sp - 1];
-      --sp;
-      __syncwarp();
-      const B* X = bufp(sm, A, g.buf);
-      B* Y = bufp(sm, A, g.buf ^ 1u);
-      const uint32_t n = g.e - g.s;
-      if (n <= (uint32_t)C::TINY) {
-        warp_sort_smem(X, A, g.s, n);
-#ifdef GQS_PROFILE
-        if (tid0_of_cta()) lp[4] += 1;
-#endif
-        continue;
+    LRec& r = sm.lrec[ri];
+    const uint32_t rs = r.s, re = r.e, buf = r.buf;
+    const B p = (B)r.pivot;
+    const B* X = bufp(sm, A, buf);
+    B* Y = bufp(sm, A, buf ^ 1u);
+    const uint32_t s0 = rs + c * (uint32_t)C::SLICE;
+    B k[C::SLICE_KPL];
+    if (s0 + (uint32_t)C::SLICE <= re) {
+#pragma unroll
+      for (int j = 0; j < C::SLICE_KPL; ++j) k[j] = X[s0 + (uint32_t)(j * 32 + lane)];
+    } else {  // the segment's last, partial slice: the pivot value pads it and is dropped
+#pragma unroll
+      for (int j = 0; j < C::SLICE_KPL; ++j) {
+        const uint32_t i = s0 + (uint32_t)(j * 32 + lane);
+        k[j] = i < re ? X[i] : p;
       }
-#ifdef GQS_PROFILE
-      if (tid0_of_cta()) lp[3] += 1;
-#endif
-      const B p = sample32_smem(X, g.s, n);
-      uint32_t lpos = g.s, gpos = g.e;
-      for (uint32_t base = g.s; base < g.e; base += 32) {
-        const uint32_t i = base + lane;
-        const bool valid = i < g.e;
-        const B kk = valid ? X[i] : B(0);
-        const bool isl = valid && kk < p, isg = valid && kk > p;
-        const uint32_t bl = __ballot_sync(0xffffffffu, isl), bg = __ballot_sync(0xffffffffu, isg);
-        if (isl) Y[lpos + __popc(bl & ltm)] = kk;
-        if (isg) Y[gpos - 1 - __popc(bg & ltm)] = kk;
-        lpos += __popc(bl);
-        gpos -= __popc(bg);
-      }
-      __syncwarp();
-      for (uint32_t i = lpos + lane; i < gpos; i += 32) A[i] = p;
-      // children [g.s, lpos) and [gpos, g.e), both in Y
-      const uint32_t cb = g.buf ^ 1u;
-      const uint32_t nl = lpos - g.s, ng = g.e - gpos;
-      int t = sp;
-      if (lane == 0) {
-        if (nl == 1 && cb) A[g.s] = Y[g.s];
-        if (ng == 1 && cb) A[gpos] = Y[gpos];
-        // larger first so the smaller child is popped next (stack depth <= log2 n + 1)
-        const Seg big = nl >= ng ? Seg{g.s, lpos, cb} : Seg{gpos, g.e, cb};
-        const Seg sml = nl >= ng ? Seg{gpos, g.e, cb} : Seg{g.s, lpos, cb};
-        if (big.e - big.s > 1) {
-          if (t < C::WSTACK) stk[t++] = big;
-          else set_error(q, ST_INTERNAL, 0x57ACull);
-        }
-        if (sml.e - sml.s > 1) {
-          if (t < C::WSTACK) stk[t++] = sml;
-          else set_error(q, ST_INTERNAL, 0x57ACull);
-        }
-      }
-      sp = __shfl_sync(0xffffffffu, t, 0);
-      __syncwarp();
     }
+    uint32_t cl = 0, cg = 0;
+#pragma unroll
+    for (int j = 0; j < C::SLICE_KPL; ++j) {
+      cl += k[j] < p;
+      cg += k[j] > p;
+    }
+    const uint32_t wl = __reduce_add_sync(0xffffffffu, cl), wg = __reduce_add_sync(0xffffffffu, cg);
+    uint32_t ol = 0, og = 0;
+    if (lane == 0) {
+      ol = atomicAdd(&r.lt, wl);
+      og = atomicAdd(&r.gt, wg);
+    }
+    ol = __shfl_sync(0xffffffffu, ol, 0);
+    og = __shfl_sync(0xffffffffu, og, 0);
+    uint32_t lpos = rs + ol, gpos = re - 1u - og;
+#pragma unroll
+    for (int j = 0; j < C::SLICE_KPL; ++j) {
+      const bool isl = k[j] < p, isg = k[j] > p;
+      const uint32_t bl = __ballot_sync(0xffffffffu, isl), bg = __ballot_sync(0xffffffffu, isg);
+      if (isl || isg) Y[isl ? lpos + __popc(bl & ltm) : gpos - __popc(bg & ltm)] = k[j];
+      lpos += __popc(bl);
+      gpos -= __popc(bg);
+    }
+    __syncwarp();
+    uint32_t last = 0;
+    if (lane == 0) {
+      __threadfence_block();
+      last = atomicSub(&r.remaining, 1u) == 1u;
+    }
+    last = __shfl_sync(0xffffffffu, last, 0);
+    if (!last) return;
+    __threadfence_block();
+    // every slice is scattered: [rs, rs+L) < p <= ... < [re-G, re) in Y, pivot run to A
+    const uint32_t L = *(volatile uint32_t*)&r.lt, G = *(volatile uint32_t*)&r.gt;
+    for (uint32_t i = rs + L + lane; i < re - G; i += 32) A[i] = p;
+    __syncwarp();
+    uint32_t fin = (re - G) - (rs + L);
+    fin += place_child(a, sm, A, rs, rs + L, buf ^ 1u, lp);
+    fin += place_child(a, sm, A, re - G, re, buf ^ 1u, lp);
+    if (lane == 0) atomicAdd(&sm.ls_done, fin);
+#ifdef GQS_PROFILE
+    if (lane == 0) lp[6] += 1;
+#endif
   }
 
-  // CTA-wide local sort of A[0, m) (keys already mapped to comparison keys). On return A
-  // holds the sorted keys. (lqsort_kernel, QuicksortKernels.cl:267-421.)
-  // lp (profile builds): {CTA-phase cycles, warp-phase cycles, CTA partitions, warp partitions,
-  // register sorts}; the leader thread's view.
-  static __device__ void local_sort(const SortArgs<T>& a, Smem<C>& sm, B* A, uint32_t m, unsigned long long* lp) {
+  // Sorts A[0, m) (comparison keys) with all consumer warps. On return A holds the keys sorted.
+  static __device__ __noinline__ void local_sort(const SortArgs<T>& a, Smem<C>& sm, B* A, uint32_t m,
+                                                 unsigned long long* lp) {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 #ifdef GQS_PROFILE
-    const long long t_cta = clock64();
+    const long long t0 = clock64();
 #endif
-    const uint32_t ltm = lanemask_lt();
     if (tid == 0) {
-      sm.csp = 0;
-      sm.wl_n = 0;
-      sm.wl_next = 0;
-      if (m > (uint32_t)C::WARP_MAX) {
-        sm.cstack[sm.csp++] = Seg{0, m, 0};
-      } else {
-        sm.wlist[sm.wl_n++] = Seg{0, m, 0};
-      }
+      sm.lr_head = 0;
+      sm.lr_tail = 0;
+      sm.ls_done = 0;
     }
+    for (uint32_t i = tid; i < (uint32_t)C::LREC; i += C::NC) sm.lrec[i].seq = 0u;
     cbar();
+    if (warp == 0) {
+      const uint32_t fin = place_child(a, sm, A, 0, m, 0u, lp);
+      if (lane == 0 && fin) atomicAdd(&sm.ls_done, fin);
+    }
+    // every warp takes slices until every key of the tile is placed
+    uint32_t spins = 0;
     for (;;) {
-      const int sp = sm.csp;
-      if (sp == 0) break;
-      const Seg g = sm.cstack[sp - 1];
-      cbar();
-      if (tid == 0) sm.csp = sp - 1;
-      const B* X = bufp(sm, A, g.buf);
-      B* Y = bufp(sm, A, g.buf ^ 1u);
-      const uint32_t n = g.e - g.s;
-      if (n <= (uint32_t)C::TINY) {
-        if (warp == 0) warp_sort_smem(X, A, g.s, n);
-        cbar();
-        continue;
-      }
-#ifdef GQS_PROFILE
-      lp[2] += 1;
-#endif
-      if (warp == 0) {
-        const B pv = sample32_smem(X, g.s, n);
-        if (lane == 0) sm.pivot_bc = (unsigned long long)pv;
-      }
-      cbar();
-      const B p = (B)sm.pivot_bc;
-      uint32_t cl = 0, cg = 0;
-      for (uint32_t i = g.s + tid; i < g.e; i += C::NC) {
-        const B kk = X[i];
-        cl += kk < p;
-        cg += kk > p;
-      }
-      cl = __reduce_add_sync(0xffffffffu, cl);
-      cg = __reduce_add_sync(0xffffffffu, cg);
+      uint32_t ri = 0, c = 0, state = 0;  // 0 nothing yet, 1 slice, 2 done
       if (lane == 0) {
-        sm.wlt[0][warp] = cl;
-        sm.wgt[0][warp] = cg;
-      }
-      cbar();
-      uint32_t vl = lane < C::NCW ? sm.wlt[0][lane] : 0u, vg = lane < C::NCW ? sm.wgt[0][lane] : 0u;
-      uint32_t il = vl, ig = vg;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t tl = __shfl_up_sync(0xffffffffu, il, o), tg = __shfl_up_sync(0xffffffffu, ig, o);
-        if (lane >= o) {
-          il += tl;
-          ig += tg;
+        const uint32_t h = *(volatile uint32_t*)&sm.lr_head;
+        const uint32_t t = *(volatile uint32_t*)&sm.lr_tail;
+        if (h < t && h < (uint32_t)C::LREC) {
+          if (*(volatile uint32_t*)&sm.lrec[h].seq == h + 1u) {
+            const uint32_t cc = atomicAdd(&sm.lrec[h].cursor, 1u);
+            if (cc < sm.lrec[h].nsl) {
+              ri = h;
+              c = cc;
+              state = 1;
+            } else {
+              atomicCAS(&sm.lr_head, h, h + 1u);
+              state = 3;  // retry at once
+            }
+          }
+        } else if (*(volatile uint32_t*)&sm.ls_done >= m) {
+          state = 2;
+        } else if (h >= (uint32_t)C::LREC) {
+          state = 2;  // record overflow was reported; stop
+        }
+        if (state == 0) {
+          if (++spins > (1u << 24) || ((spins & 1023u) == 0u && ld_relaxed(&a.q->error))) {
+            set_error(a.q, ST_TIMEOUT, 0x15ull);
+            state = 2;
+          } else {
+            __nanosleep(128);
+          }
         }
       }
-      const uint32_t L = __shfl_sync(0xffffffffu, il, 31), G = __shfl_sync(0xffffffffu, ig, 31);
-      uint32_t lpos = g.s + __shfl_sync(0xffffffffu, il - vl, warp);
-      uint32_t gpos = g.e - G + __shfl_sync(0xffffffffu, ig - vg, warp);
-      // same strided order as the count pass, so each warp's ranks stay within its range
-      for (uint32_t base = g.s; base < g.e; base += C::NC) {
-        const uint32_t i = base + tid;
-        const bool valid = i < g.e;
-        const B kk = valid ? X[i] : B(0);
-        const bool isl = valid && kk < p, isg = valid && kk > p;
-        const uint32_t bl = __ballot_sync(0xffffffffu, isl), bg = __ballot_sync(0xffffffffu, isg);
-        if (isl) Y[lpos + __popc(bl & ltm)] = kk;
-        if (isg) Y[gpos + __popc(bg & ltm)] = kk;
-        lpos += __popc(bl);
-        gpos += __popc(bg);
-      }
-      cbar();
-      for (uint32_t i = g.s + L + tid; i < g.e - G; i += C::NC) A[i] = p;
-      if (tid == 0) {
-        const uint32_t cb = g.buf ^ 1u;
-        const uint32_t ls = g.s, le = g.s + L, gs = g.e - G, ge = g.e;
-        if (L >= G) {
-          push_child(sm, A, ls, le, cb, a.q);
-          push_child(sm, A, gs, ge, cb, a.q);
-        } else {
-          push_child(sm, A, gs, ge, cb, a.q);
-          push_child(sm, A, ls, le, cb, a.q);
-        }
-      }
-      cbar();
-    }
-    // warp phase
+      state = __shfl_sync(0xffffffffu, state, 0);
+      if (state == 2) break;
+      if (state != 1) continue;
+      ri = __shfl_sync(0xffffffffu, ri, 0);
+      c = __shfl_sync(0xffffffffu, c, 0);
+      __threadfence_block();
 #ifdef GQS_PROFILE
-    const long long t_warp = clock64();
-    lp[0] += (unsigned long long)(t_warp - t_cta);
+      const long long ts = clock64();
 #endif
-    const int nwl = sm.wl_n;
-    for (;;) {
-      int idx = 0;
-      if (lane == 0) idx = atomicAdd(&sm.wl_next, 1);
-      idx = __shfl_sync(0xffffffffu, idx, 0);
-      if (idx >= nwl) break;
-      warp_quicksort(sm, A, sm.wlist[idx], sm.wstack[warp], a.q, lp);
+      run_slice(a, sm, A, ri, c, lp);
+#ifdef GQS_PROFILE
+      if (lane == 0) lp[5] += (unsigned long long)(clock64() - ts);
+#endif
     }
     cbar();
 #ifdef GQS_PROFILE
-    lp[1] += (unsigned long long)(clock64() - t_warp);
+    if (tid == 0) lp[1] += (unsigned long long)(clock64() - t0);
 #endif
   }
 
@@ -1030,7 +1149,6 @@ struct Persistent {
     uint32_t pend_len = 0, pend_job = 0, pend_par = 0, scat_job = 0;
     B pend_p = 0;
     B* pend_dst = nullptr;
-    unsigned long long pend_lb = 0, pend_gb = 0;  // leader only
     unsigned long long st_part = 0, st_local = 0, st_chunks = 0;
     uint32_t st_local_jobs = 0, st_fill_jobs = 0;
     GQS_PROF_DECL
@@ -1046,17 +1164,38 @@ struct Persistent {
       (void)mbar_test(&sm.full[s], (k / C::STAGES) & 1u);  // completed; gives this thread acquire order
       const Desc dd = sm.desc[s];
       if (dd.kind == ITEM_PART) {
-        const B* stg = sm.stage[s] + dd.off;
+        // The stage holds the chunk's 16-byte granules: keys [off, off + len) of an aligned
+        // window of CHUNK keys. Each thread reads 16-byte vectors; positions outside the chunk
+        // take the pivot's value, which neither side counts or keeps.
         const B p = (B)dd.pivot;
         B cur[C::KPT];
+        constexpr int VEC = 16 / (int)sizeof(B);
+        const uint4* win = reinterpret_cast<const uint4*>(sm.stage[s]);
+#pragma unroll
+        for (int v = 0; v < C::KPT / VEC; ++v) {
+          const uint4 w = win[v * C::NC + tid];
+          B t[VEC];
+          memcpy(t, &w, 16);
+#pragma unroll
+          for (int q = 0; q < VEC; ++q) cur[v * VEC + q] = t[q];
+        }
+        if (dd.off != 0 || dd.len != (uint32_t)C::CHUNK) {
+          const B praw = Ops::raw(p);
+#pragma unroll
+          for (int v = 0; v < C::KPT / VEC; ++v) {
+#pragma unroll
+            for (int q = 0; q < VEC; ++q) {
+              const uint32_t idx = (uint32_t)((v * C::NC + tid) * VEC + q);
+              if (idx < dd.off || idx >= dd.off + dd.len) cur[v * VEC + q] = praw;
+            }
+          }
+        }
         uint32_t cl = 0, cg = 0;
 #pragma unroll
         for (int j = 0; j < C::KPT; ++j) {
-          const uint32_t i = (uint32_t)(j * C::NC + tid);
-          cur[j] = i < dd.len ? stg[i] : B(0);
           const B kk = Ops::key(cur[j]);
-          cl += (i < dd.len) && kk < p;
-          cg += (i < dd.len) && kk > p;
+          cl += kk < p;
+          cg += kk > p;
         }
         const uint32_t par = npart % 3u;
         cl = __reduce_add_sync(0xffffffffu, cl);
@@ -1065,38 +1204,43 @@ struct Persistent {
           sm.wlt[par][warp] = cl;
           sm.wgt[par][warp] = cg;
         }
+        GQS_PROF_ADD(PF_C_COUNT, t_it)
         cbar();  // #1: stage s read into registers; the previous scatter is complete
-        unsigned long long new_lb = 0, new_gb = 0;
+        GQS_PROF_T(t_l)
         if (tid == 0) {
           mbar_arrive(&sm.empty[s]);
           if (have_scat) post_chunk(a, sm, scat_job);
-          if (have_pend) {
-            sm.blt[pend_par] = pend_lb;
-            sm.bgt[pend_par] = pend_gb;
-          }
           uint32_t ls = 0, gs = 0;
 #pragma unroll
           for (int w = 0; w < C::NCW; ++w) {
             ls += sm.wlt[par][w];
             gs += sm.wgt[par][w];
           }
-          // Reserve this chunk's output ranges in the parent (QuicksortKernels.cl:183-186).
-          // The results are used one iteration later, hiding the atomic round trip.
-          Job* j = a.jobs + dd.job;
-          new_lb = atomicAdd(&j->sstart, (unsigned long long)ls);
-          new_gb = atomicAdd(&j->send, (unsigned long long)(-(long long)gs)) - gs;
+          // Ask the reserver warp for this chunk's output ranges; they are used one iteration
+          // later, when this chunk is scattered.
+          const uint32_t e = npart % C::RQ;
+          sm.rq_job[e] = dd.job;
+          sm.rq_ls[e] = ls;
+          sm.rq_gs[e] = gs;
+          sts_release(&sm.rq_tail, npart + 1);
+          bool ok = !have_pend || leader_wait_reservation(a, sm, npart - 1);
           GQS_PROF_T(tw)
           leader_wait_slot(a, sm, k + 1);
+          if (!ok) sm.cons_ok = 0;
           GQS_PROF_ADD(PF_C_WAIT, tw)
         }
-        cbar();  // #2: bases of the pending chunk published; next slot verdict published
+        cbar();  // #2: the pending chunk's ranges are reserved; next slot verdict published
+        GQS_PROF_ADD(PF_C_LEADER, t_l)
+        if (!sm.cons_ok) break;
+        GQS_PROF_T(t_sc)
         have_scat = false;
         if (have_pend) {
-          scatter_chunk(pend, pend_len, pend_p, pend_dst, sm.blt[pend_par], sm.bgt[pend_par], sm.wlt[pend_par],
-                        sm.wgt[pend_par]);
+          const uint32_t e = (npart - 1) % C::RQ;
+          scatter_chunk(pend, pend_p, pend_dst, sm.rs_lb[e], sm.rs_gb[e], sm.wlt[pend_par], sm.wgt[pend_par]);
           have_scat = true;
           scat_job = pend_job;
         }
+        GQS_PROF_ADD(PF_C_SCATTER, t_sc)
 #pragma unroll
         for (int j = 0; j < C::KPT; ++j) pend[j] = cur[j];
         pend_len = dd.len;
@@ -1104,8 +1248,6 @@ struct Persistent {
         pend_par = par;
         pend_p = p;
         pend_dst = dd.dir ? a.dn : a.d;
-        pend_lb = new_lb;
-        pend_gb = new_gb;
         have_pend = true;
         st_part += dd.len;
         ++st_chunks;
@@ -1118,15 +1260,13 @@ struct Persistent {
       // Any other item first drains the pipeline of partition chunks.
       if (tid == 0) {
         if (have_scat) post_chunk(a, sm, scat_job);
-        if (have_pend) {
-          sm.blt[pend_par] = pend_lb;
-          sm.bgt[pend_par] = pend_gb;
-        }
+        if (have_pend && !leader_wait_reservation(a, sm, npart - 1)) sm.cons_ok = 0;
       }
       cbar();
+      if (!sm.cons_ok) break;
       if (have_pend) {
-        scatter_chunk(pend, pend_len, pend_p, pend_dst, sm.blt[pend_par], sm.bgt[pend_par], sm.wlt[pend_par],
-                      sm.wgt[pend_par]);
+        const uint32_t e = (npart - 1) % C::RQ;
+        scatter_chunk(pend, pend_p, pend_dst, sm.rs_lb[e], sm.rs_gb[e], sm.wlt[pend_par], sm.wgt[pend_par]);
       }
       cbar();
       if (tid == 0) {
@@ -1161,13 +1301,21 @@ struct Persistent {
           for (uint32_t i = tid; i < m; i += C::NC) A[i] = Ops::key(A[i]);
           cbar();
         }
-        unsigned long long lp[5] = {0, 0, 0, 0, 0};
+        unsigned long long lp[14] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
         local_sort(a, sm, A, m, lp);
         GQS_PROF_CNT(PF_C_LCTA, lp[0])
         GQS_PROF_CNT(PF_C_LWARP, lp[1])
         GQS_PROF_CNT(PF_N_LCTA, lp[2])
         GQS_PROF_CNT(PF_N_LWARP, lp[3])
         GQS_PROF_CNT(PF_N_LBIT, lp[4])
+#ifdef GQS_PROFILE
+        if (lane == 0) {  // per-warp totals of the warp phase
+          atomicAdd(&a.q->prof[PF_W_WAIT], lp[5]);
+          atomicAdd(&a.q->prof[PF_W_PART], lp[6]);
+          atomicAdd(&a.q->prof[PF_W_BIT], lp[7]);
+          atomicAdd(&a.q->prof[PF_W_SEGS], lp[8]);
+        }
+#endif
         GQS_PROF_CNT(PF_N_LOCAL, 1)
         GQS_PROF_T(ts)
 
@@ -1241,6 +1389,8 @@ __global__ void __launch_bounds__(C::NT, 1) persistent_kernel(SortArgs<typename 
     sm.cq_head = 0;
     sm.cq_tail = 0;
     sm.term = 0;
+    sm.rq_tail = 0;
+    for (int i = 0; i < C::RQ; ++i) sm.rs_done[i] = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
@@ -1249,8 +1399,10 @@ __global__ void __launch_bounds__(C::NT, 1) persistent_kernel(SortArgs<typename 
     Persistent<C>::consumers(a, sm);
   } else if (warp == C::NCW) {
     Persistent<C>::producer(a, sm);
-  } else {
+  } else if (warp == C::NCW + 1) {
     Persistent<C>::completer(a, sm);
+  } else {
+    Persistent<C>::reserver(a, sm);
   }
 }
 

@@ -4,14 +4,14 @@
 namespace gqs {
 
 // Cfg<T, consumer warps, tile keys, chunk keys, stages, keys per lane in the register sort, warp-phase max>
-using f32_v0 = Cfg<float, 16, 16384, 4096, 4, 8, 1024>;
+using f32_v0 = Cfg<float, 16, 12288, 8192, 3, 8, 4096>;
 
 int variant_count_f32() { return 1; }
 
 VariantInfo variant_info_f32(int v) {
   switch (v) {
     default:
-      return VariantOps<f32_v0>::info("f32_ncw16_tile16384_chunk4096");
+      return VariantOps<f32_v0>::info("f32_ncw16_tile12288_chunk8192");
   }
 }
 

@@ -4,14 +4,14 @@
 namespace gqs {
 
 // Cfg<T, consumer warps, tile keys, chunk keys, stages, keys per lane in the register sort, warp-phase max>
-using u32_v0 = Cfg<uint32_t, 16, 16384, 4096, 4, 8, 1024>;
+using u32_v0 = Cfg<uint32_t, 16, 12288, 8192, 3, 8, 4096>;
 
 int variant_count_u32() { return 1; }
 
 VariantInfo variant_info_u32(int v) {
   switch (v) {
     default:
-      return VariantOps<u32_v0>::info("u32_ncw16_tile16384_chunk4096");
+      return VariantOps<u32_v0>::info("u32_ncw16_tile12288_chunk8192");
   }
 }
 

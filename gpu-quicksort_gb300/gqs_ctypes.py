@@ -201,7 +201,8 @@ class Context:
 
     PROFILE_SLOTS = ["c_wait", "c_part", "c_drain", "c_lwait", "c_lcta", "c_lwarp", "c_lstore", "c_fill",
                      "p_grab", "p_empty", "p_lempty", "p_idle", "q_busy", "q_idle", "n_local", "c_total",
-                     "p_issue", "n_grab", "n_lcta", "n_lwarp", "n_lbit", "n_items"]
+                     "p_issue", "n_grab", "n_lcta", "n_lwarp", "n_lbit", "n_items", "c_count", "c_leader",
+                     "c_scatter", "w_slice", "n_segs", "w_bit"]
 
     def profile(self) -> dict:
         buf = (C.c_uint64 * 32)()
