@@ -57,3 +57,22 @@ struct VariantOps {
 
 }  // namespace gqs
 
+// Defines info_/prepare_/launch_<S>_<V> for the table entry whose index equals WANT.
+#define GQS_DEFINE_VARIANT_IF(S, V, WANT, T, NCW, TILE, CHUNK, STAGES, R, WM)                     \
+  GQS_DEFINE_VARIANT_IF_##V##_##WANT(S, V, T, NCW, TILE, CHUNK, STAGES, R, WM)
+#define GQS_DEFINE_VARIANT_BODY(S, V, T, NCW, TILE, CHUNK, STAGES, R, WM)                         \
+  using S##_##V##_cfg = Cfg<T, NCW, TILE, CHUNK, STAGES, R, WM>;                                    \
+  VariantInfo info_##S##_##V() {                                                                   \
+    return VariantOps<S##_##V##_cfg>::info(#S "_ncw" #NCW "_tile" #TILE "_chunk" #CHUNK "_st" #STAGES); \
+  }                                                                                                \
+  int prepare_##S##_##V() { return VariantOps<S##_##V##_cfg>::prepare(); }                         \
+  cudaError_t launch_##S##_##V(const LaunchParams& p) { return VariantOps<S##_##V##_cfg>::launch(p); }
+#define GQS_DEFINE_VARIANT_IF_0_0(...) GQS_DEFINE_VARIANT_BODY(__VA_ARGS__)
+#define GQS_DEFINE_VARIANT_IF_1_1(...) GQS_DEFINE_VARIANT_BODY(__VA_ARGS__)
+#define GQS_DEFINE_VARIANT_IF_2_2(...) GQS_DEFINE_VARIANT_BODY(__VA_ARGS__)
+#define GQS_DEFINE_VARIANT_IF_0_1(...)
+#define GQS_DEFINE_VARIANT_IF_0_2(...)
+#define GQS_DEFINE_VARIANT_IF_1_0(...)
+#define GQS_DEFINE_VARIANT_IF_1_2(...)
+#define GQS_DEFINE_VARIANT_IF_2_0(...)
+#define GQS_DEFINE_VARIANT_IF_2_1(...)

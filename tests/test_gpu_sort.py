@@ -207,3 +207,22 @@ def test_full_size_configs(gpu_ctx, dtype, dist, n):
     assert st["status"] == 0 and st["keys"] == n
     del t, ref, got
     torch.cuda.empty_cache()
+
+
+# ---------------------------------------------------------------------------
+# every compiled kernel variant sorts correctly
+
+@pytest.mark.parametrize("dtype", ["u32", "f32", "f64"])
+def test_all_variants(dtype):
+    for v in gqs_ctypes.variants(dtype):
+        ctx = gqs_ctypes.Context(variant=v["index"], timing=True)
+        try:
+            for dist in ("uniform", "distinct16", "sorted"):
+                for n in (3000, v["tile"] + 1, 3 * v["chunk"] + 17, 1_500_007):
+                    a = gqs_ctypes.generate(dtype, dist if dtype == "u32" or dist != "uniform" else "uniform", 31 + n, n)
+                    b = a.copy()
+                    ctx.sort(b)
+                    assert np.array_equal(b.view(np.uint8), oracle_sorted(a).view(np.uint8)), (v["name"], dist, n)
+                    assert ctx.stats()["variant"] == v["index"]
+        finally:
+            ctx.close()
