@@ -105,7 +105,7 @@ class ClockSampler:
         try:
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={index}", f"--query-gpu={q}", "--format=csv,noheader,nounits",
-                                          "-lms", "100"], stdout=self.f, stderr=subprocess.DEVNULL)
+                                          "-lms", "50"], stdout=self.f, stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
 
@@ -257,6 +257,9 @@ def main():
         if rc != 0:
             raise RuntimeError(f"sort enqueue failed: {gqs_ctypes.STATUS.get(rc, rc)}")
 
+    # clocks are sampled from the warm-up on (the sampler needs ~0.2 s to start), through the
+    # timed steps
+    clocks = ClockSampler(enabled=(not args.no_clocks and rank == 0), index=local)
     for _ in range(args.warmup):
         d.copy_(pristine)
         sort_once()
@@ -277,7 +280,6 @@ def main():
         del got, ref
     torch.cuda.empty_cache()
 
-    clocks = ClockSampler(enabled=(not args.no_clocks and rank == 0), index=local)
     ev0 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ev1 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     kernel_ms, algo_bytes, stats_last = [], [], None
