@@ -24,7 +24,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
               "--expt-relaxed-constexpr", "-I" + CSRC, "-I" + INCLUDE]
 CU_SOURCES = ["gqs_v_%s_%d.cu" % (t, v) for t in ("u32", "f32", "f64") for v in range(3)] + \
-    ["gqs_sort_dispatch.cu", "gqs_capi.cu"]
+    ["gqs_sort_dispatch.cu", "gqs_capi.cu", "gqs_noalloc.cu"]
 
 LIB = os.path.join(HERE, "libgqs.so")
 PROF_LIB = os.path.join(HERE, "libgqs_prof.so")  # -DGQS_PROFILE: per-role cycle counters

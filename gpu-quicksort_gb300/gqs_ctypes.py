@@ -30,7 +30,7 @@ EXPORTS = [
     "gqs_sort_u32_dev", "gqs_sort_f32_dev", "gqs_sort_f64_dev",
     "gqs_sort_segments_u32_dev", "gqs_sort_segments_f32_dev", "gqs_sort_segments_f64_dev",
     "gqs_sort_segments_u32", "gqs_sort_segments_f32", "gqs_sort_segments_f64",
-    "gqs_sync", "gqs_last_stats", "gqs_last_profile", "gqs_variant_count", "gqs_variant_describe", "gqs_set_variant",
+    "gqs_sort_u32_noalloc", "gqs_sync", "gqs_last_stats", "gqs_last_profile", "gqs_variant_count", "gqs_variant_describe", "gqs_set_variant",
     "gqs_get_variant", "gqs_strerror", "gqs_version",
 ]
 
@@ -99,6 +99,8 @@ def load_library(path: str | None = None) -> C.CDLL:
         f = getattr(lib, f"gqs_sort_segments_{t}")
         f.argtypes = [vp, vp, sz, vp, sz]
         f.restype = st
+    lib.gqs_sort_u32_noalloc.argtypes = [vp, sz, vp]
+    lib.gqs_sort_u32_noalloc.restype = st
     lib.gqs_sync.argtypes = [vp]
     lib.gqs_sync.restype = st
     lib.gqs_last_stats.argtypes = [vp, C.POINTER(Stats)]

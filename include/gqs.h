@@ -118,6 +118,22 @@ gqs_status gqs_sort_segments_u32(gqs_ctx* ctx, uint32_t* keys, size_t n, const u
 gqs_status gqs_sort_segments_f32(gqs_ctx* ctx, float* keys, size_t n, const uint64_t* offsets, size_t nseg);
 gqs_status gqs_sort_segments_f64(gqs_ctx* ctx, double* keys, size_t n, const uint64_t* offsets, size_t nseg);
 
+/* Largest n accepted by gqs_sort_u32_noalloc. */
+#define GQS_NOALLOC_MAX_KEYS (1u << 20)
+
+/* Sort that allocates nothing, for callers that must not allocate device memory when they sort:
+ * hosts that give all device memory to their own pool at start-up and forbid allocations later,
+ * and latency-critical code that cannot take cudaMalloc's implicit device synchronisation.
+ * Such callers cannot create a gqs_ctx (its pools are cudaMalloc'd), so this call takes none.
+ * Sorts d (device memory, n <= GQS_NOALLOC_MAX_KEYS uint32 keys) in place on the current
+ * device and `stream`, waits, and returns the device status; larger n returns GQS_ERR_INVALID
+ * before any work. All of its scratch is one static device array inside the library (about
+ * 6 MB, held by every GPU that loads the library until the process exits) shared by every call:
+ * calls that overlap on the GPU race, so the caller serialises them. The first call on a device
+ * looks up that array's address and prepares the kernel; make it before any stream capture.
+ * No counterpart in the reference, which allocates its buffers per call. */
+gqs_status gqs_sort_u32_noalloc(uint32_t* d, size_t n, void* stream);
+
 /* Waits for the context's last enqueued sort and returns its device status. */
 gqs_status gqs_sync(gqs_ctx* ctx);
 
