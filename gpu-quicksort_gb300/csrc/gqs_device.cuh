@@ -1108,8 +1108,6 @@ struct Persistent {
           if (++spins > (1u << 24) || ((spins & 1023u) == 0u && ld_relaxed(&a.q->error))) {
             set_error(a.q, ST_TIMEOUT, 0x15ull);
             state = 2;
-          } else {
-            __nanosleep(128);
           }
         }
       }
