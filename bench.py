@@ -44,7 +44,7 @@ def parse():
     p.add_argument("--steps", type=int, default=5)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--config", default="plain", choices=["plain", "batched", "tiles"])
+    p.add_argument("--config", default="plain", choices=["plain", "batched", "tiles", "serve"])
     p.add_argument("--dtype", default="u32", choices=["u32", "f32", "f64"])
     p.add_argument("--dist", default="uniform")
     p.add_argument("--log2n", type=int, default=28)
@@ -53,6 +53,10 @@ def parse():
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-clocks", action="store_true")
     p.add_argument("--profile", action="store_true", help="use libgqs_prof.so and print its cycle counters")
+    p.add_argument("--serve-requests", type=int, default=20000,
+                   help="requests of the serving stream (--config serve, and the summary in the plain line; 0: skip)")
+    p.add_argument("--serve-load", type=float, default=0.7,
+                   help="Poisson offered load as a fraction of the batched server's measured capacity")
     return p.parse_args()
 
 
@@ -197,6 +201,308 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+class CudaView:
+    """Exposes a raw device pointer to torch.as_tensor (no copy)."""
+
+    def __init__(self, ptr, n, typestr):
+        self.__cuda_array_interface__ = {"shape": (n,), "typestr": typestr, "data": (ptr, False), "version": 2}
+
+
+# ---------------------------------------------------------------------------
+# Serving stream: 60/30/10 % u32/f32/f64 requests, sizes log-uniform in [2^10, 2^24]
+
+SERVE_DIST = {"u32": "uniform", "f32": "gaussian", "f64": "uniform"}
+SERVE_TYPES = ("u32", "f32", "f64")
+
+
+class OutPool:
+    """Ring allocator over one pinned host buffer for request outputs (client-side window)."""
+
+    def __init__(self, nbytes):
+        import collections
+        import threading
+        import torch
+        self.buf = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+        self.base = self.buf.data_ptr()
+        self.size = nbytes
+        self.head = 0
+        self.live = collections.deque()  # [start, end, done] in allocation order
+        self.cv = threading.Condition()
+
+    def alloc(self, nbytes):
+        nbytes = (nbytes + 255) // 256 * 256
+        with self.cv:
+            while True:
+                while self.live and self.live[0][2]:
+                    self.live.popleft()
+                if not self.live:
+                    self.head = 0
+                    lo, hi = 0, self.size
+                else:
+                    first = self.live[0][0]
+                    lo, hi = (self.head, self.size) if self.head > first else (self.head, first)
+                    if self.head > first and lo + nbytes > hi:
+                        lo, hi = 0, first  # wrap
+                if lo + nbytes <= hi:
+                    rec = [lo, lo + nbytes, False]
+                    self.live.append(rec)
+                    self.head = lo + nbytes
+                    return rec
+                self.cv.wait()
+
+    def free(self, rec):
+        with self.cv:
+            rec[2] = True
+            self.cv.notify_all()
+
+
+def serve_stream(count, seed):
+    rng = np.random.default_rng(seed)
+    u = rng.random(count)
+    dt = np.where(u < 0.6, 0, np.where(u < 0.9, 1, 2))
+    n = np.exp(rng.uniform(np.log(2.0 ** 10), np.log(2.0 ** 24), count)).astype(np.int64)
+    src = (rng.integers(0, 1 << 20, count) // 64) * 64
+    return dt, n, src
+
+
+def run_serve_arm(gqs_ctypes, templates, stream, per_request, rate, pool, sample_every=97):
+    """Runs the stream through one server. rate None: saturation (submit as fast as the output
+    window allows); else Poisson arrivals at `rate` requests/s. Returns latencies and samples."""
+    import threading
+    dt, n, src = stream
+    count = len(n)
+    srv = gqs_ctypes.Server(budget_bytes=64 << 30, batch_keys=1 << 27, batch_segments=4096, lanes=3,
+                            per_request=per_request)
+    esz = [4, 4, 8]
+    arrive = np.zeros(count)
+    if rate:
+        arrive = np.cumsum(np.random.default_rng(12345).exponential(1.0 / rate, count))
+    info = [None] * count
+    recs = [None] * count
+    idx_of = {}
+    samples = {}
+    lock = threading.Lock()
+
+    def collect():
+        got = 0
+        while got < count:
+            code, rid, inf = srv.wait_any(60000)
+            if code == 4 and rid == 0:
+                raise RuntimeError("serving stream stalled")
+            with lock:
+                i = idx_of.pop(rid)
+            if code != 0:
+                raise RuntimeError(f"request {i} failed: {gqs_ctypes.STATUS.get(code, code)}")
+            info[i] = inf
+            if i % sample_every == 0 and n[i] <= (1 << 21):
+                a = np.frombuffer(pool.buf.numpy(), dtype=gqs_ctypes.NP_DTYPES[SERVE_TYPES[dt[i]]],
+                                  count=int(n[i]), offset=recs[i][0])
+                samples[i] = a.copy()
+            pool.free(recs[i])
+            got += 1
+
+    col = threading.Thread(target=collect)
+    col.start()
+    t0 = srv.now_ns()
+    t_wall0 = time.perf_counter()
+    for i in range(count):
+        if rate:
+            delay = arrive[i] - (time.perf_counter() - t_wall0)
+            if delay > 0:
+                time.sleep(delay)
+        t = SERVE_TYPES[dt[i]]
+        nb = int(n[i]) * esz[dt[i]]
+        rec = pool.alloc(nb)
+        recs[i] = rec
+        tmpl = templates[t]
+        with lock:
+            rid = srv.submit_raw(t, tmpl.data_ptr() + int(src[i]) * esz[dt[i]], pool.base + rec[0], int(n[i]))
+            idx_of[rid] = i
+    col.join()
+    st = srv.stats()
+    srv.close()
+    done = np.array([x["t_done_ns"] for x in info], dtype=np.float64)
+    sub = np.array([x["t_submit_ns"] for x in info], dtype=np.float64)
+    arr_ns = t0 + arrive * 1e9 if rate else sub
+    lat_ms = (done - np.minimum(arr_ns, sub)) / 1e6
+    span = (done.max() - min(t0, sub.min())) / 1e9
+    return {"keys_per_s": float(n.sum()) / span, "span_s": span, "lat_ms": lat_ms,
+            "batches": st["batches"], "max_batch_requests": st["max_batch_requests"],
+            "arena_peak_gb": st["arena_peak"] / 1e9}, samples
+
+
+def run_serve(args, gqs_ctypes):
+    """The serving comparison: batched server vs per-request plain sorts on the same stream."""
+    import torch
+    count = args.serve_requests
+    stream = serve_stream(count, SEED)
+    dt, n, src = stream
+    templates = {}
+    for k, t in enumerate(SERVE_TYPES):
+        tdt = {"u32": torch.int32, "f32": torch.float32, "f64": torch.float64}[t]
+        buf = torch.empty((1 << 24) + (1 << 20), dtype=tdt, pin_memory=True)
+        v = buf.numpy().view(gqs_ctypes.NP_DTYPES[t])
+        gqs_ctypes.generate(t, SERVE_DIST[t], SEED + 7 * k, v.size, out=v)
+        templates[t] = buf
+    pool = OutPool(3 << 30)
+    # warm-up: a short stream through both modes (graph capture, pool growth)
+    warm = serve_stream(64, SEED + 1)
+    run_serve_arm(gqs_ctypes, templates, warm, False, None, pool)
+    run_serve_arm(gqs_ctypes, templates, warm, True, None, pool)
+    sat_b, samp_b = run_serve_arm(gqs_ctypes, templates, stream, False, None, pool)
+    sat_p, samp_p = run_serve_arm(gqs_ctypes, templates, stream, True, None, pool)
+    mean_keys = float(n.mean())
+    rate = args.serve_load * sat_b["keys_per_s"] / mean_keys
+    poi_b, _ = run_serve_arm(gqs_ctypes, templates, stream, False, rate, pool)
+    poi_p, _ = run_serve_arm(gqs_ctypes, templates, stream, True, rate, pool)
+    # bit-exact checks on the sampled requests: both modes, against numpy's sort of the input
+    ok = True
+    for i, a in samp_b.items():
+        t = SERVE_TYPES[dt[i]]
+        ref = np.sort(templates[t].numpy().view(gqs_ctypes.NP_DTYPES[t])[src[i]:src[i] + n[i]])
+        ok &= bool(np.array_equal(a.view(np.uint8), ref.view(np.uint8)))
+        if i in samp_p:
+            ok &= bool(np.array_equal(a.view(np.uint8), samp_p[i].view(np.uint8)))
+
+    def lat(r):
+        return {"p50_ms": float(np.percentile(r["lat_ms"], 50)), "p99_ms": float(np.percentile(r["lat_ms"], 99)),
+                "gkeys_s": r["keys_per_s"] / 1e9, "span_s": r["span_s"], "batches": r["batches"]}
+
+    total_keys = int(n.sum())
+    in_bytes = int(sum(int(n[i]) * (8 if dt[i] == 2 else 4) for i in range(count)))
+    return {
+        "requests": count, "keys": total_keys, "bytes_each_way": in_bytes,
+        "mix": "60/30/10 % u32/f32/f64", "sizes": "log-uniform in [2^10, 2^24]",
+        "values": "u32 uniform, f32 N(0, 1e3), f64 U[-1e9, 1e9]",
+        "server": {"budget_gb": 64, "lanes": 3, "batch_keys": 1 << 27, "batch_segments": 4096},
+        "host_buffers": "pinned inputs and outputs",
+        "saturation": {"batched_gkeys_s": sat_b["keys_per_s"] / 1e9, "per_request_gkeys_s": sat_p["keys_per_s"] / 1e9,
+                       "speedup": sat_b["keys_per_s"] / sat_p["keys_per_s"], "batched_batches": sat_b["batches"],
+                       "batched_max_batch_requests": sat_b["max_batch_requests"],
+                       "batched_arena_peak_gb": sat_b["arena_peak_gb"]},
+        "poisson": {"offered_load": f"{args.serve_load:.2f} x batched capacity", "rate_req_s": rate,
+                    "offered_gkeys_s": rate * mean_keys / 1e9, "batched": lat(poi_b), "per_request": lat(poi_p)},
+        "check": {"sampled_requests": len(samp_b), "bit_exact_vs_numpy_and_per_request": ok},
+    }
+
+
+def run_batched(args, gqs_ctypes, rank, local, world, dist, barrier):
+    """4096 uint32 arrays, lengths log-uniform in [32, 2^20], as one graph-captured batch."""
+    import torch
+    nseg = 4096
+    off = gqs_ctypes.segment_offsets(SEED + rank, nseg, 32, 1 << 20)
+    n = int(off[-1])
+    esize = 4
+    host_in = torch.empty(n, dtype=torch.int32, pin_memory=True)
+    hv = host_in.numpy().view(np.uint32)
+    gqs_ctypes.generate("u32", "uniform", SEED + rank, n, out=hv)
+    batch = gqs_ctypes.Batch("u32", n, nseg, device=local, variant=args.variant)
+    batch.set_segments(off)
+    batch.copy_in(hv)
+    arena = torch.as_tensor(CudaView(batch.keys_ptr, n, "<i4"), device="cuda")
+    pristine = host_in.cuda()
+    tune = None
+    if args.variant < 0:
+        best, ms = batch.autotune(nseg, reps=2)
+        tune = {"chosen": gqs_ctypes.variants("u32")[best]["name"],
+                "median_ms": {gqs_ctypes.variants("u32")[v]["name"]: m for v, m in enumerate(ms)}}
+    stream = torch.cuda.current_stream()
+    clocks = ClockSampler(enabled=(not args.no_clocks and rank == 0), index=local)
+
+    def step():
+        rc = batch.launch(nseg, stream.cuda_stream)
+        if rc != 0:
+            raise RuntimeError(f"batch launch failed: {gqs_ctypes.STATUS.get(rc, rc)}")
+
+    for _ in range(args.warmup):
+        arena.copy_(pristine)
+        step()
+        code, st = batch.wait()
+        if code != 0:
+            raise RuntimeError(f"batch failed: {st}")
+    # correctness: (segment, key) pairs sorted lexicographically equal the batch's output
+    seg_id = torch.repeat_interleave(torch.arange(nseg, device="cuda", dtype=torch.int64),
+                                     torch.from_numpy(np.diff(off).astype(np.int64)).cuda())
+    keyed = (seg_id << 32) | (pristine.to(torch.int64) & 0xFFFFFFFF)
+    ref = torch.sort(keyed).values & 0xFFFFFFFF
+    check = {"bit_exact_vs_torch_sort_per_segment": bool(torch.equal(arena.to(torch.int64) & 0xFFFFFFFF, ref))}
+    del seg_id, keyed, ref
+    ev0 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ev1 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    kms, abytes = [], []
+    barrier()
+    torch.cuda.synchronize()
+    for i in range(args.steps):
+        arena.copy_(pristine)
+        ev0[i].record(stream)
+        step()
+        ev1[i].record(stream)
+        code, st = batch.wait()
+        if code != 0:
+            raise RuntimeError(f"batch failed: {st}")
+        kms.append(st["kernel_ms"])
+        abytes.append(st["algo_bytes"])
+    torch.cuda.synchronize()
+    barrier()
+    clk = clocks.stop()
+    t = sum(a.elapsed_time(b) for a, b in zip(ev0, ev1)) / 1e3
+    value = n * world * args.steps / t / 1e9
+    # end to end through the public batch calls: pinned host -> arena, replay, arena -> host
+    out = torch.empty_like(host_in, pin_memory=True)
+    ov = out.numpy().view(np.uint32)
+    times = []
+    for i in range(args.steps + 1):
+        t0 = time.perf_counter()
+        batch.copy_in(hv)
+        step()
+        code, _ = batch.wait()
+        batch.copy_out(ov)
+        if i:
+            times.append(time.perf_counter() - t0)
+    e2e = {"value": n * args.steps / sum(times) / 1e9, "unit": "Gkeys/s", "h2d_bytes_per_step": n * esize,
+           "d2h_bytes_per_step": n * esize, "ms_per_step": 1e3 * sum(times) / args.steps,
+           "api": "gqs_batch_copy_in + gqs_batch_launch + gqs_batch_wait + gqs_batch_copy_out (pinned)"}
+    # the same arrays sorted by one plain call each (device pointers, enqueued back to back)
+    ctx = gqs_ctypes.Context(device=local, sync=False, timing=False, variant=0)
+    d = pristine.clone()
+    dn = torch.empty_like(d)
+    ctx.reserve("u32", int(np.diff(off).max()), 1)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for i in range(nseg):
+        rc = ctx.sort_dev("u32", d.data_ptr() + int(off[i]) * 4, dn.data_ptr() + int(off[i]) * 4,
+                          int(off[i + 1] - off[i]), stream.cuda_stream)
+        if rc != 0:
+            raise RuntimeError("plain sort failed")
+    e1.record(stream)
+    torch.cuda.synchronize()
+    plain_ms = e0.elapsed_time(e1)
+    plain_same = bool(torch.equal(d, arena))
+    ctx.close()
+    if rank != 0:
+        return None
+    peak, peak_src = measured_peak()
+    km, ab = float(np.mean(kms)), float(np.mean(abytes))
+    achieved = ab / (km / 1e3) / 1e9
+    return {
+        "metric": f"Gkeys/s ({workload_name(args, n)})", "value": value, "unit": "Gkeys/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+        "data": "synthetic (seeded generator, gpu-quicksort_gb300/workload)",
+        "config": {"workload": workload_name(args, n), "keys": n, "segments": nseg, "seed": SEED,
+                   "l2": "inputs larger than L2 (arena rewritten from a pristine copy before every step)",
+                   "variant": gqs_ctypes.variants("u32")[batch.variant]["name"], "graph": "one cudaGraphLaunch per step",
+                   "parallelism": f"replicas x{world}"},
+        "autotune": tune,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": ncu_traffic("batched_u32"), "kernel": "gqs::persistent_kernel (graph replay)",
+                     "kernel_ms": km, "algo_bytes_per_launch": ab, "peak_source": peak_src},
+        "plain_per_array": {"gkeys_s": n / (plain_ms / 1e3) / 1e9, "ms": plain_ms, "calls": nseg,
+                            "same_output": plain_same},
+        "cpu_baseline": None, "e2e": e2e, "gpu_launches": 2 * args.steps, "clocks": clk, "check": check,
+    }
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -220,18 +526,37 @@ def main():
         if dist is not None:
             dist.barrier()
 
+    if args.config == "batched":
+        line = run_batched(args, gqs_ctypes, rank, local, world, dist, barrier)
+        if line is not None:
+            print(json.dumps(line), flush=True)
+        if dist is not None:
+            dist.destroy_process_group()
+        return
+    if args.config == "serve":
+        if rank == 0:
+            sv = run_serve(args, gqs_ctypes)
+            line = {"metric": "Gkeys/s (serving stream, batched server, saturation)",
+                    "value": sv["saturation"]["batched_gkeys_s"], "unit": "Gkeys/s", "n_gpus": 1,
+                    "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "mixed u32/f32/f64",
+                    "data": "synthetic (seeded generator, gpu-quicksort_gb300/workload)",
+                    "config": {"workload": "serving stream of mixed sort requests"}, "serve": sv,
+                    "e2e": {"value": sv["saturation"]["batched_gkeys_s"], "unit": "Gkeys/s",
+                            "h2d_bytes_per_step": sv["bytes_each_way"], "d2h_bytes_per_step": sv["bytes_each_way"],
+                            "step": "the whole stream"}}
+            print(json.dumps(line), flush=True)
+        if dist is not None:
+            dist.destroy_process_group()
+        return
+
     tdt = {"u32": torch.int32, "f32": torch.float32, "f64": torch.float64}[args.dtype]
     npdt = gqs_ctypes.NP_DTYPES[args.dtype]
     esize = np.dtype(npdt).itemsize
 
     # ---- input
     offsets = None
-    nseg = 4096
-    if args.config == "batched":
-        off = gqs_ctypes.segment_offsets(SEED + rank, nseg, 32, 1 << 20)
-        n = int(off[-1])
-        offsets = torch.from_numpy(off.astype(np.int64)).cuda()
-    elif args.config == "tiles":
+    nseg = 1
+    if args.config == "tiles":
         nseg = (1 << args.log2n) // 8000
         off = np.arange(nseg + 1, dtype=np.int64) * (6000 if args.dtype == "f64" else 8000)
         n = int(off[-1])
@@ -240,7 +565,7 @@ def main():
         n = 1 << args.log2n
     host_in = torch.empty(n, dtype=tdt, pin_memory=True)
     hv = host_in.numpy().view(npdt) if args.dtype == "u32" else host_in.numpy()
-    gqs_ctypes.generate(args.dtype, args.dist if args.config != "batched" else "uniform", SEED + rank, n, out=hv)
+    gqs_ctypes.generate(args.dtype, args.dist, SEED + rank, n, out=hv)
     pristine = host_in.cuda()
     d = torch.empty_like(pristine)
     dn = torch.empty_like(pristine)
@@ -350,6 +675,11 @@ def main():
                 "per_unit": f"{esize} B x 2 per key per pass (partition chunks + on-chip sort + register sort)"}
     cpu = None if args.no_cpu else cpu_baseline(args, n)
     v0 = gqs_ctypes.variants(args.dtype)[stats_last["variant"]]
+    serve = None
+    if args.config == "plain" and args.serve_requests > 0 and world == 1:
+        del d, dn, pristine
+        torch.cuda.empty_cache()
+        serve = run_serve(args, gqs_ctypes)
     line = {
         "metric": METRIC if (args.config == "plain" and args.log2n == 28 and args.dtype == "u32")
         else f"Gkeys/s ({workload_name(args, n)})",
@@ -369,6 +699,7 @@ def main():
         "stats": {k: stats_last[k] for k in ("part_keys", "local_keys", "tiny_keys", "fill_keys", "chunks",
                                              "part_jobs", "local_jobs", "fill_chunks", "max_depth")},
         "passes_per_key": (stats_last["part_keys"] + stats_last["local_keys"] + stats_last["tiny_keys"]) / n,
+        "serve": serve,
         "profile": ctx.profile() if args.profile else None,
         "wall_s": wall,
     }

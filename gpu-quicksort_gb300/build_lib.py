@@ -23,8 +23,8 @@ INCLUDE = os.path.join(ROOT, "include")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
               "--expt-relaxed-constexpr", "-I" + CSRC, "-I" + INCLUDE]
-CU_SOURCES = ["gqs_v_%s_%d.cu" % (t, v) for t in ("u32", "f32", "f64") for v in range(3)] + \
-    ["gqs_sort_dispatch.cu", "gqs_capi.cu", "gqs_noalloc.cu"]
+CU_SOURCES = ["gqs_sort_dispatch.cu", "gqs_capi.cu", "gqs_noalloc.cu", "gqs_batch.cu", "gqs_serve.cu"]
+VARIANT_TU = "gqs_variant_tu.cu"  # compiled once per (key type, variant index)
 
 LIB = os.path.join(HERE, "libgqs.so")
 PROF_LIB = os.path.join(HERE, "libgqs_prof.so")  # -DGQS_PROFILE: per-role cycle counters
@@ -57,6 +57,26 @@ def _headers() -> list[str]:
     return hs
 
 
+def variant_count() -> int:
+    """Variants per key type, as gqs_variant_table.h defines them."""
+    with open(os.path.join(CSRC, "gqs_variant_table.h")) as f:
+        for line in f:
+            if line.startswith("#define GQS_VARIANT_COUNT"):
+                return int(line.split()[2])
+    raise RuntimeError("GQS_VARIANT_COUNT not found")
+
+
+def _units() -> list[tuple[str, str, list[str]]]:
+    """(source, object name, extra flags) of every CUDA translation unit."""
+    units = [(src, src.replace(".cu", ".o"), []) for src in CU_SOURCES]
+    for t in ("u32", "f32", "f64"):
+        for v in range(variant_count()):
+            units.append((VARIANT_TU, "gqs_v_%s_%d.o" % (t, v),
+                          ["-DGQS_TU_LIST=GQS_VARIANTS_" + t.upper(), "-DGQS_TU_TYPE=" + t,
+                           "-DGQS_TU_INDEX=%d" % v]))
+    return units
+
+
 def build(force: bool = False, verbose: bool = False, profile: bool = False) -> dict:
     """Compiles what is out of date; returns the library paths. profile=True builds
     libgqs_prof.so with the device cycle counters instead of libgqs.so."""
@@ -68,19 +88,19 @@ def build(force: bool = False, verbose: bool = False, profile: bool = False) -> 
     headers = _headers()
     jobs = []
     objs = []
-    for src in CU_SOURCES:
+    for src, obj, defs in _units():
         s = os.path.join(CSRC, src)
-        o = os.path.join(bdir, src.replace(".cu", ".o"))
+        o = os.path.join(bdir, obj)
         objs.append(o)
         if force or _stale(o, [s] + headers):
-            jobs.append([nvcc] + ARCH + NVCC_FLAGS + extra + ["-c", s, "-o", o])
+            jobs.append([nvcc] + ARCH + NVCC_FLAGS + extra + defs + ["-c", s, "-o", o])
     wsrc = os.path.join(HERE, "workload", "gqs_workload.cpp")
     whdr = os.path.join(HERE, "workload", "gqs_workload.h")
     wjob = None
     if force or _stale(WORKLOAD_LIB, [wsrc, whdr]):
         wjob = ["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off",
                 "-fno-fast-math", "-I" + os.path.join(HERE, "workload"), wsrc, "-o", WORKLOAD_LIB]
-    with cf.ThreadPoolExecutor(max_workers=max(1, min(8, os.cpu_count() or 1))) as ex:
+    with cf.ThreadPoolExecutor(max_workers=max(1, min(16, os.cpu_count() or 1))) as ex:
         futs = [ex.submit(_run, j) for j in jobs]
         if wjob:
             futs.append(ex.submit(_run, wjob))

@@ -15,6 +15,7 @@
 
 #include "gqs.h"
 #include "gqs_device.cuh"
+#include "gqs_host.h"
 #include "gqs_launch.h"
 
 namespace gqs {
@@ -54,19 +55,11 @@ cudaError_t launch_sort(int dtype, const LaunchParams& p) {
 namespace {
 
 constexpr int kMaxVariants = 16;
-constexpr size_t kElemSize[3] = {4, 4, 8};
-
-struct DeviceGuard {
-  int prev = -1;
-  explicit DeviceGuard(int dev) {
-    if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
-    if (prev != dev) cudaSetDevice(dev);
-  }
-  ~DeviceGuard() {
-    int cur = -1;
-    if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
-  }
-};
+using gqs::cuda_status;
+using gqs::DeviceGuard;
+using gqs::job_capacity;
+using gqs::kElemSize;
+using gqs::ticket_ring;
 
 }  // namespace
 
@@ -103,12 +96,6 @@ struct gqs_ctx {
 
 namespace {
 
-gqs_status cuda_status(cudaError_t e) {
-  if (e == cudaSuccess) return GQS_OK;
-  if (e == cudaErrorMemoryAllocation) return GQS_ERR_NOMEM;
-  return GQS_ERR_CUDA;
-}
-
 // Grows a device buffer to at least `bytes`; callers have waited for pending work.
 gqs_status grow(void** p, size_t* cap, size_t bytes) {
   if (*cap >= bytes && *p) return GQS_OK;
@@ -126,23 +113,6 @@ gqs_status grow(void** p, size_t* cap, size_t bytes) {
   return GQS_OK;
 }
 
-// Job records one sort can need: local jobs are disjoint ranges longer than `tiny` keys,
-// partition jobs ranges longer than `tile` keys (with generous room for uneven pivots), plus
-// one root per segment and the fill jobs of long pivot runs.
-size_t job_capacity(const gqs::VariantInfo& vi, size_t n, size_t nseg) {
-  return n / (size_t)vi.tiny + 16 * (n / (size_t)vi.tile) + n / 32768 + 2 * nseg + 4096;
-}
-
-// Ticket-ring entries: tickets not yet taken belong to live jobs, whose ranges are disjoint,
-// so they number at most the chunks of n keys (plus one partial chunk per job) plus one per
-// local job and fill chunk.
-size_t ticket_ring(const gqs::VariantInfo& vi, size_t n, size_t nseg) {
-  size_t need = 2 * (n / (size_t)vi.chunk) + n / (size_t)vi.tiny + n / 32768 + 2 * nseg + 65536;
-  size_t r = 1;
-  while (r < need) r <<= 1;
-  return r;
-}
-
 gqs_status wait_pending_locked(gqs_ctx* c) {
   if (!c->pending) return GQS_OK;
   cudaError_t e = cudaEventSynchronize(c->ev_done);
@@ -150,31 +120,13 @@ gqs_status wait_pending_locked(gqs_ctx* c) {
   e = cudaMemcpy(c->q_host, c->q, sizeof(gqs::Queue), cudaMemcpyDeviceToHost);
   c->pending = false;
   if (e != cudaSuccess) return cuda_status(e);
-  const gqs::Queue& q = *c->q_host;
-  gqs_stats s{};
-  s.keys = q.total;
-  s.part_keys = q.part_keys;
-  s.local_keys = q.local_keys;
-  s.tiny_keys = q.tiny_keys;
-  s.fill_keys = q.fill_keys;
-  s.chunks = q.chunks;
-  s.algo_bytes = kElemSize[c->pending_dtype] * 2 * (q.part_keys + q.local_keys + q.tiny_keys);
-  s.part_jobs = q.part_jobs;
-  s.local_jobs = q.local_jobs;
-  s.fill_chunks = q.fill_jobs;
-  s.max_depth = q.max_depth;
-  s.status = q.error;
-  s.variant = (uint32_t)c->pending_variant;
-  s.grid = (uint32_t)c->pending_grid;
-  s.threads = (uint32_t)gqs::variant_info(c->pending_dtype, c->pending_variant).threads;
-  s.kernel_ms = -1.0;
+  gqs_stats s = gqs::stats_from_queue(*c->q_host, c->pending_dtype, c->pending_variant, c->pending_grid);
   if (c->pending_timed) {
     float ms = 0.f;
     if (cudaEventElapsedTime(&ms, c->ev_begin, c->ev_end) == cudaSuccess) s.kernel_ms = ms;
   }
-  if (q.error == 0 && q.done != q.total) s.status = GQS_ERR_INTERNAL;
   c->last = s;
-  for (int i = 0; i < 32; ++i) c->last_prof[i] = q.prof[i];
+  for (int i = 0; i < 32; ++i) c->last_prof[i] = c->q_host->prof[i];
   return (gqs_status)s.status;
 }
 
@@ -362,19 +314,13 @@ void gqs_config_default(gqs_config* cfg) {
 gqs_status gqs_create(gqs_ctx** out, int device, const gqs_config* cfg) {
   if (!out) return GQS_ERR_INVALID;
   *out = nullptr;
-  int ndev = 0;
-  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) {
-    (void)cudaGetLastError();
-    return GQS_ERR_NO_DEVICE;
-  }
-  if (device < 0 || device >= ndev) return GQS_ERR_INVALID;
-  cudaDeviceProp prop;
-  if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) return GQS_ERR_NO_DEVICE;
-  if (prop.major != 10 || prop.minor != 3) return GQS_ERR_NO_DEVICE;  // built for sm_103a only
+  int num_sms = 0;
+  const gqs_status dst = gqs::check_device(device, &num_sms);
+  if (dst != GQS_OK) return dst;
   gqs_ctx* c = new (std::nothrow) gqs_ctx();
   if (!c) return GQS_ERR_NOMEM;
   c->device = device;
-  c->num_sms = prop.multiProcessorCount;
+  c->num_sms = num_sms;
   gqs_config_default(&c->cfg);
   if (cfg) c->cfg = *cfg;
   DeviceGuard dg(device);

@@ -474,13 +474,26 @@ __device__ unsigned long long dispatch_range(const SortArgs<typename C::T>& a, u
 // ---------------------------------------------------------------------------
 // Seed kernel: one warp per segment turns the segment table into root jobs.
 
+// Segment i is [offsets[i], offsets[i+1]) or, with `pairs`, [offsets[2i], offsets[2i+1]) (the
+// segments then need not be adjacent); without offsets, the one segment [0, n). Every segment
+// must lie in [0, n).
 template <class C>
 __global__ void __launch_bounds__(256) seed_kernel(SortArgs<typename C::T> a, const unsigned long long* offsets,
-                                                   uint32_t nseg, unsigned long long n) {
+                                                   const unsigned long long* nseg_dev, uint32_t nseg,
+                                                   unsigned long long n, uint32_t pairs) {
   const uint32_t seg = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
+  if (nseg_dev) {  // a replayable launch: the count is data, at most the launch's capacity
+    const unsigned long long m = *nseg_dev;
+    if (m > nseg) {
+      if (seg == 0 && lane == 0) set_error(a.q, ST_INVALID, m);
+      return;
+    }
+    nseg = (uint32_t)m;
+  }
   if (seg >= nseg) return;
-  const unsigned long long s = offsets ? offsets[seg] : 0ull, e = offsets ? offsets[seg + 1] : n;
+  const unsigned long long s = offsets ? offsets[pairs ? 2ull * seg : seg] : 0ull;
+  const unsigned long long e = offsets ? offsets[pairs ? 2ull * seg + 1 : seg + 1] : n;
   if (s > e || e > n) {  // malformed segment table
     if (lane == 0) set_error(a.q, ST_INVALID, seg);
     return;
@@ -1372,8 +1385,15 @@ struct Persistent {
   }
 };
 
+// CTAs per SM the kernel is compiled for: two when two CTAs' shared memory fits an SM (the
+// register budget per thread halves accordingly), else one.
 template <class C>
-__global__ void __launch_bounds__(C::NT, 1) persistent_kernel(SortArgs<typename C::T> a) {
+constexpr int min_blocks_per_sm() {
+  return sizeof(Smem<C>) <= 110u * 1024u ? 2 : 1;
+}
+
+template <class C>
+__global__ void __launch_bounds__(C::NT, min_blocks_per_sm<C>()) persistent_kernel(SortArgs<typename C::T> a) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   Smem<C>& sm = *reinterpret_cast<Smem<C>*>(smem_raw);
   const int tid = threadIdx.x;

@@ -1,5 +1,5 @@
-// Internal launch interface between the C ABI (gqs_capi.cu) and the per-key-type
-// translation units that instantiate the kernels (gqs_sort_{u32,f32,f64}.cu).
+// Internal launch interface between the C ABI (gqs_capi.cu, gqs_batch.cu) and the
+// translation units that instantiate the kernels (gqs_variant_tu.cu, one per variant).
 #pragma once
 #include <cstddef>
 #include <cstdint>
@@ -34,8 +34,10 @@ struct LaunchParams {
   uint32_t tmask;
   unsigned long long timeout_ns;
   const unsigned long long* offsets;  // nseg + 1 device offsets, or null for one segment [0, n)
-  unsigned long long n;               // keys when offsets is null
-  uint32_t nseg;
+  unsigned long long n;               // keys when offsets is null; else the bound of every offset
+  uint32_t nseg;                      // segments (with nseg_dev: the most the launch may see)
+  const unsigned long long* nseg_dev; // optional: segment count read on the device (replayable graphs)
+  uint32_t pairs;                     // 1: offsets holds (start, end) per segment, 2 * nseg entries
   int variant;
   int grid;
   cudaStream_t stream;
@@ -43,7 +45,7 @@ struct LaunchParams {
   cudaEvent_t ev_end;
 };
 
-// Per key type (defined in gqs_sort_<type>.cu).
+// Per key type (defined in gqs_sort_dispatch.cu).
 #define GQS_DECLARE_TYPE(S)                         \
   int variant_count_##S();                          \
   VariantInfo variant_info_##S(int v);              \

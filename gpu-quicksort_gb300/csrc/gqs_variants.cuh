@@ -1,5 +1,5 @@
-// Kernel variants per key type and the code that launches one. Each translation unit
-// gqs_sort_<type>.cu includes this file once for its key type.
+// The code that describes, prepares and launches one kernel variant (a Cfg). Each
+// compilation of gqs_variant_tu.cu instantiates it for one entry of gqs_variant_table.h.
 #pragma once
 #include "gqs_device.cuh"
 #include "gqs_launch.h"
@@ -44,7 +44,7 @@ struct VariantOps {
     a.timeout_ns = p.timeout_ns;
     const uint32_t nseg = p.offsets ? p.nseg : 1u;
     const uint32_t seed_blocks = (nseg + 7u) / 8u;  // 8 warps per 256-thread block, one per segment
-    seed_kernel<C><<<seed_blocks, 256, 0, p.stream>>>(a, p.offsets, nseg, p.n);
+    seed_kernel<C><<<seed_blocks, 256, 0, p.stream>>>(a, p.offsets, p.nseg_dev, nseg, p.n, p.pairs);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     if (p.ev_begin) cudaEventRecord(p.ev_begin, p.stream);
@@ -56,23 +56,3 @@ struct VariantOps {
 };
 
 }  // namespace gqs
-
-// Defines info_/prepare_/launch_<S>_<V> for the table entry whose index equals WANT.
-#define GQS_DEFINE_VARIANT_IF(S, V, WANT, T, NCW, TILE, CHUNK, STAGES, R, WM)                     \
-  GQS_DEFINE_VARIANT_IF_##V##_##WANT(S, V, T, NCW, TILE, CHUNK, STAGES, R, WM)
-#define GQS_DEFINE_VARIANT_BODY(S, V, T, NCW, TILE, CHUNK, STAGES, R, WM)                         \
-  using S##_##V##_cfg = Cfg<T, NCW, TILE, CHUNK, STAGES, R, WM>;                                    \
-  VariantInfo info_##S##_##V() {                                                                   \
-    return VariantOps<S##_##V##_cfg>::info(#S "_ncw" #NCW "_tile" #TILE "_chunk" #CHUNK "_st" #STAGES); \
-  }                                                                                                \
-  int prepare_##S##_##V() { return VariantOps<S##_##V##_cfg>::prepare(); }                         \
-  cudaError_t launch_##S##_##V(const LaunchParams& p) { return VariantOps<S##_##V##_cfg>::launch(p); }
-#define GQS_DEFINE_VARIANT_IF_0_0(...) GQS_DEFINE_VARIANT_BODY(__VA_ARGS__)
-#define GQS_DEFINE_VARIANT_IF_1_1(...) GQS_DEFINE_VARIANT_BODY(__VA_ARGS__)
-#define GQS_DEFINE_VARIANT_IF_2_2(...) GQS_DEFINE_VARIANT_BODY(__VA_ARGS__)
-#define GQS_DEFINE_VARIANT_IF_0_1(...)
-#define GQS_DEFINE_VARIANT_IF_0_2(...)
-#define GQS_DEFINE_VARIANT_IF_1_0(...)
-#define GQS_DEFINE_VARIANT_IF_1_2(...)
-#define GQS_DEFINE_VARIANT_IF_2_0(...)
-#define GQS_DEFINE_VARIANT_IF_2_1(...)

@@ -32,6 +32,10 @@ EXPORTS = [
     "gqs_sort_segments_u32", "gqs_sort_segments_f32", "gqs_sort_segments_f64",
     "gqs_sort_u32_noalloc", "gqs_sync", "gqs_last_stats", "gqs_last_profile", "gqs_variant_count", "gqs_variant_describe", "gqs_set_variant",
     "gqs_get_variant", "gqs_strerror", "gqs_version",
+    "gqs_batch_create", "gqs_batch_destroy", "gqs_batch_keys", "gqs_batch_offsets", "gqs_batch_launch",
+    "gqs_batch_wait", "gqs_batch_copy_in", "gqs_batch_copy_out", "gqs_batch_set_variant", "gqs_batch_get_variant", "gqs_batch_autotune",
+    "gqs_srv_config_default", "gqs_srv_create", "gqs_srv_destroy", "gqs_srv_submit", "gqs_srv_wait",
+    "gqs_srv_wait_any", "gqs_srv_drain", "gqs_srv_stats", "gqs_srv_now_ns",
 ]
 
 
@@ -61,6 +65,30 @@ class Stats(C.Structure):
 class VariantDesc(C.Structure):
     _fields_ = [("threads", C.c_int32), ("tile", C.c_int32), ("chunk", C.c_int32), ("kpt", C.c_int32),
                 ("stages", C.c_int32), ("tiny", C.c_int32), ("smem_bytes", C.c_uint64), ("name", C.c_char * 64)]
+
+
+class ServerConfig(C.Structure):
+    _fields_ = [("budget_bytes", C.c_uint64), ("batch_keys", C.c_uint64), ("batch_segments", C.c_uint32),
+                ("lanes", C.c_uint32), ("timeout_ms", C.c_uint32), ("per_request", C.c_uint32),
+                ("variant", C.c_int32 * 3), ("reserved", C.c_uint32 * 4)]
+
+
+class RequestInfo(C.Structure):
+    _fields_ = [("status", C.c_uint32), ("dtype", C.c_uint32), ("n", C.c_uint64), ("t_submit_ns", C.c_uint64),
+                ("t_admit_ns", C.c_uint64), ("t_launch_ns", C.c_uint64), ("t_done_ns", C.c_uint64),
+                ("batch_requests", C.c_uint32), ("lane", C.c_uint32)]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+class ServerStats(C.Structure):
+    _fields_ = [(k, C.c_uint64) for k in ("submitted", "completed", "failed", "completed_keys", "batches",
+                                          "max_batch_requests", "arena_bytes", "arena_used", "arena_peak",
+                                          "pending", "outstanding")]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
 
 
 _lib = None
@@ -119,6 +147,46 @@ def load_library(path: str | None = None) -> C.CDLL:
     lib.gqs_strerror.restype = C.c_char_p
     lib.gqs_version.argtypes = []
     lib.gqs_version.restype = C.c_int
+    lib.gqs_batch_create.argtypes = [C.c_int, C.c_int, sz, sz, C.POINTER(Config), C.POINTER(vp)]
+    lib.gqs_batch_create.restype = st
+    lib.gqs_batch_destroy.argtypes = [vp]
+    lib.gqs_batch_destroy.restype = None
+    lib.gqs_batch_keys.argtypes = [vp]
+    lib.gqs_batch_keys.restype = vp
+    lib.gqs_batch_offsets.argtypes = [vp]
+    lib.gqs_batch_offsets.restype = C.POINTER(C.c_uint64)
+    lib.gqs_batch_launch.argtypes = [vp, sz, vp]
+    lib.gqs_batch_launch.restype = st
+    lib.gqs_batch_wait.argtypes = [vp, C.POINTER(Stats)]
+    lib.gqs_batch_wait.restype = st
+    lib.gqs_batch_copy_in.argtypes = [vp, vp, sz, sz]
+    lib.gqs_batch_copy_in.restype = st
+    lib.gqs_batch_copy_out.argtypes = [vp, vp, sz, sz]
+    lib.gqs_batch_copy_out.restype = st
+    lib.gqs_batch_set_variant.argtypes = [vp, C.c_int]
+    lib.gqs_batch_set_variant.restype = st
+    lib.gqs_batch_get_variant.argtypes = [vp]
+    lib.gqs_batch_get_variant.restype = C.c_int
+    lib.gqs_batch_autotune.argtypes = [vp, sz, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_int)]
+    lib.gqs_batch_autotune.restype = st
+    lib.gqs_srv_config_default.argtypes = [C.POINTER(ServerConfig)]
+    lib.gqs_srv_config_default.restype = None
+    lib.gqs_srv_create.argtypes = [C.c_int, C.POINTER(ServerConfig), C.POINTER(vp)]
+    lib.gqs_srv_create.restype = st
+    lib.gqs_srv_destroy.argtypes = [vp]
+    lib.gqs_srv_destroy.restype = None
+    lib.gqs_srv_submit.argtypes = [vp, C.c_int, vp, vp, sz, C.POINTER(C.c_uint64)]
+    lib.gqs_srv_submit.restype = st
+    lib.gqs_srv_wait.argtypes = [vp, C.c_uint64, C.POINTER(RequestInfo)]
+    lib.gqs_srv_wait.restype = st
+    lib.gqs_srv_wait_any.argtypes = [vp, C.POINTER(C.c_uint64), C.POINTER(RequestInfo), C.c_uint32]
+    lib.gqs_srv_wait_any.restype = st
+    lib.gqs_srv_drain.argtypes = [vp]
+    lib.gqs_srv_drain.restype = st
+    lib.gqs_srv_stats.argtypes = [vp, C.POINTER(ServerStats)]
+    lib.gqs_srv_stats.restype = st
+    lib.gqs_srv_now_ns.argtypes = []
+    lib.gqs_srv_now_ns.restype = C.c_uint64
     if path is None:
         _lib = lib
     return lib
@@ -216,6 +284,164 @@ class Context:
 
     def get_variant(self, dtype: str) -> int:
         return self.lib.gqs_get_variant(self.h, DTYPES[dtype])
+
+
+class Batch:
+    """A graph-captured batched segmented sort (gqs_batch_*): the caller fills the device key
+    arena (`keys_ptr`) and the pinned segment table (`offsets`), then launches."""
+
+    def __init__(self, dtype: str, max_keys: int, max_segments: int, device: int = 0, variant: int = -1,
+                 timeout_ms: int = 4000):
+        self.lib = load_library()
+        self.dtype = dtype
+        cfg = Config()
+        self.lib.gqs_config_default(C.byref(cfg))
+        cfg.variant = variant
+        cfg.timeout_ms = timeout_ms
+        h = C.c_void_p()
+        _check(self.lib.gqs_batch_create(device, DTYPES[dtype], max_keys, max_segments, C.byref(cfg), C.byref(h)),
+               "gqs_batch_create")
+        self.h = h
+        self.max_keys = max_keys
+        self.max_segments = max_segments
+        self.keys_ptr = self.lib.gqs_batch_keys(h)
+        self.offsets = np.ctypeslib.as_array(self.lib.gqs_batch_offsets(h), shape=(max_segments + 1,))
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            self.offsets = None
+            self.lib.gqs_batch_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_segments(self, offsets: np.ndarray) -> int:
+        off = np.asarray(offsets, dtype=np.uint64)
+        nseg = off.size - 1
+        if nseg > self.max_segments:
+            raise ValueError("too many segments for this batch")
+        self.offsets[: nseg + 1] = off
+        return nseg
+
+    def copy_in(self, a: np.ndarray, first: int = 0) -> None:
+        assert a.dtype == NP_DTYPES[self.dtype] and a.flags.c_contiguous
+        _check(self.lib.gqs_batch_copy_in(self.h, _ptr(a), first, a.size), "gqs_batch_copy_in")
+
+    def copy_out(self, a: np.ndarray, first: int = 0) -> None:
+        assert a.dtype == NP_DTYPES[self.dtype] and a.flags.c_contiguous
+        _check(self.lib.gqs_batch_copy_out(self.h, _ptr(a), first, a.size), "gqs_batch_copy_out")
+
+    def launch(self, nseg: int, stream: int = 0) -> int:
+        return self.lib.gqs_batch_launch(self.h, nseg, stream or None)
+
+    def wait(self) -> tuple[int, dict]:
+        s = Stats()
+        code = self.lib.gqs_batch_wait(self.h, C.byref(s))
+        return code, s.as_dict()
+
+    def set_variant(self, v: int) -> None:
+        _check(self.lib.gqs_batch_set_variant(self.h, v), "gqs_batch_set_variant")
+
+    @property
+    def variant(self) -> int:
+        return self.lib.gqs_batch_get_variant(self.h)
+
+    def autotune(self, nseg: int, reps: int = 3) -> tuple[int, list[float]]:
+        """Times every variant on the batch as it stands; selects and returns the fastest."""
+        nv = self.lib.gqs_variant_count(DTYPES[self.dtype])
+        ms = (C.c_double * nv)()
+        best = C.c_int(-1)
+        _check(self.lib.gqs_batch_autotune(self.h, nseg, reps, ms, C.byref(best)), "gqs_batch_autotune")
+        return best.value, [ms[i] for i in range(nv)]
+
+
+class Server:
+    """The continuous-batching sort server (gqs_srv_*)."""
+
+    def __init__(self, device: int = 0, budget_bytes: int = 64 << 30, batch_keys: int = 1 << 27,
+                 batch_segments: int = 4096, lanes: int = 3, per_request: bool = False,
+                 variants: tuple[int, int, int] = (-1, -1, -1), timeout_ms: int = 4000):
+        self.lib = load_library()
+        cfg = ServerConfig()
+        self.lib.gqs_srv_config_default(C.byref(cfg))
+        cfg.budget_bytes = budget_bytes
+        cfg.batch_keys = batch_keys
+        cfg.batch_segments = batch_segments
+        cfg.lanes = lanes
+        cfg.per_request = 1 if per_request else 0
+        cfg.timeout_ms = timeout_ms
+        for i, v in enumerate(variants):
+            cfg.variant[i] = v
+        h = C.c_void_p()
+        _check(self.lib.gqs_srv_create(device, C.byref(cfg), C.byref(h)), "gqs_srv_create")
+        self.h = h
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            self.lib.gqs_srv_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def submit(self, src: np.ndarray, out: np.ndarray | None = None) -> int:
+        """Queues a sort of `src` into `out` (default: in place); both must outlive the request."""
+        t = _np_tag(src)
+        out = src if out is None else out
+        assert out.dtype == src.dtype and out.size >= src.size and src.flags.c_contiguous and out.flags.c_contiguous
+        rid = C.c_uint64()
+        _check(self.lib.gqs_srv_submit(self.h, DTYPES[t], _ptr(src), _ptr(out), src.size, C.byref(rid)),
+               "gqs_srv_submit")
+        return rid.value
+
+    def submit_raw(self, dtype: str, src: int, out: int, n: int) -> int:
+        rid = C.c_uint64()
+        _check(self.lib.gqs_srv_submit(self.h, DTYPES[dtype], src, out, n, C.byref(rid)), "gqs_srv_submit")
+        return rid.value
+
+    def wait(self, rid: int) -> tuple[int, dict]:
+        info = RequestInfo()
+        code = self.lib.gqs_srv_wait(self.h, rid, C.byref(info))
+        return code, info.as_dict()
+
+    def wait_any(self, timeout_ms: int = 10000) -> tuple[int, int, dict]:
+        """(status, request id, info) of the next completed request; status 4 (timeout) when none."""
+        rid = C.c_uint64(0)
+        info = RequestInfo()
+        code = self.lib.gqs_srv_wait_any(self.h, C.byref(rid), C.byref(info), timeout_ms)
+        return code, rid.value, info.as_dict()
+
+    def drain(self) -> int:
+        return self.lib.gqs_srv_drain(self.h)
+
+    def stats(self) -> dict:
+        s = ServerStats()
+        code = self.lib.gqs_srv_stats(self.h, C.byref(s))
+        d = s.as_dict()
+        d["call_status"] = code
+        return d
+
+    def now_ns(self) -> int:
+        return self.lib.gqs_srv_now_ns()
 
 
 def variants(dtype: str) -> list[dict]:

@@ -134,6 +134,115 @@ gqs_status gqs_sort_segments_f64(gqs_ctx* ctx, double* keys, size_t n, const uin
  * No counterpart in the reference, which allocates its buffers per call. */
 gqs_status gqs_sort_u32_noalloc(uint32_t* d, size_t n, void* stream);
 
+/* ---- Batched sort, captured once as a CUDA graph ------------------------------------------
+ * A batch sorts up to max_segments independent arrays (segments) of one key type, holding up to
+ * max_keys keys in total, in one persistent launch. It owns its device memory: a key arena of
+ * max_keys keys that the caller fills (gqs_batch_keys), its scratch, the job records, ticket
+ * ring and status block. The work of one batch (copy of the segment table from pinned host
+ * memory, clearing of the status block and ring, the seed kernel, the persistent kernel, the
+ * read-back of the status block) is captured once per kernel variant as a CUDA graph;
+ * gqs_batch_launch replays it with a single cudaGraphLaunch. The segment table is data, so
+ * batches of any shape up to the maxima replay the same graph.
+ * No reference counterpart: the reference sorts one array per call
+ * (GPU-Quicksort_Full_SYCL/QuicksortMain.cpp:835-906); this is the batched form of that path. */
+typedef struct gqs_batch gqs_batch;
+
+/* cfg may be NULL; cfg->variant (>= 0) picks the initial kernel variant, cfg->timeout_ms the
+ * device-side no-progress limit. */
+gqs_status gqs_batch_create(int device, int dtype, size_t max_keys, size_t max_segments, const gqs_config* cfg,
+                            gqs_batch** out);
+void gqs_batch_destroy(gqs_batch* b);
+/* The device key arena (max_keys keys of the batch's type); segments index into it. */
+void* gqs_batch_keys(gqs_batch* b);
+/* The pinned host segment table: max_segments + 1 non-decreasing boundaries; segment i is
+ * keys[offsets[i], offsets[i+1]). Write the first nseg + 1 entries before gqs_batch_launch. */
+uint64_t* gqs_batch_offsets(gqs_batch* b);
+/* Sorts the nseg segments of the table: waits for the batch's previous replay (which reads the
+ * table), checks the table on the host, then enqueues one graph replay on `stream`. */
+gqs_status gqs_batch_launch(gqs_batch* b, size_t nseg, void* stream);
+/* Waits for the last replay; returns its device status and fills *stats (may be NULL);
+ * stats->kernel_ms is the replay's time from CUDA events. */
+gqs_status gqs_batch_wait(gqs_batch* b, gqs_stats* stats);
+/* Synchronous copies between host memory and keys [first, first + n) of the arena, for callers
+ * without CUDA bindings of their own. */
+gqs_status gqs_batch_copy_in(gqs_batch* b, const void* host, size_t first, size_t n);
+gqs_status gqs_batch_copy_out(gqs_batch* b, void* host, size_t first, size_t n);
+gqs_status gqs_batch_set_variant(gqs_batch* b, int variant);
+int gqs_batch_get_variant(gqs_batch* b);
+/* The autotuner. Times every kernel variant of the batch's key type on the batch as it stands
+ * (the first nseg segments of the table, keys restored from a copy before every replay): one
+ * warm-up replay, then `reps` timed replays, median kept. Variants differ in the partition ->
+ * on-chip sort switch (tile keys), CTA size (consumer warps) and keys per thread of a partition
+ * chunk (gqs_variant_describe). Writes each variant's median ms to ms[v] (-1: cannot run; ms may
+ * be NULL), selects the fastest for later launches and returns it in *best. On return the keys
+ * are sorted, by the chosen variant. Allocates a temporary copy of the keys. */
+gqs_status gqs_batch_autotune(gqs_batch* b, size_t nseg, int reps, double* ms, int* best);
+
+/* ---- Sort server: continuous batching of mixed requests ------------------------------------
+ * A server owns a device arena (the memory budget) and a dispatcher thread. Submitted requests
+ * (key type, host input, host output, n) are admitted in arrival order as soon as their keys
+ * and scratch fit in the free part of the arena; their keys are then copied to the device and
+ * wait there. Whenever one of `lanes` batches-in-flight is free, every resident request of one
+ * key type (oldest type first, up to batch_segments requests and batch_keys keys) is sorted as
+ * one segment of one graph-captured batch launch, and results are copied back to each
+ * request's output. Requests that arrive while others run are admitted and launched as memory
+ * and lanes free up, so copies and sorts of different batches overlap on the device. A
+ * request's result does not depend on what it was batched with. Output buffers in page-locked
+ * memory (cudaHostAlloc / cudaHostRegister) are filled asynchronously; pageable ones are filled
+ * by a synchronous copy when the batch retires. No reference counterpart. */
+typedef struct gqs_server gqs_server;
+
+typedef struct gqs_server_config {
+  uint64_t budget_bytes;   /* device memory for the server: records + keys + scratch; 0 = 64 GiB */
+  uint64_t batch_keys;     /* most keys in one batch, and in one request; 0 = 2^27 */
+  uint32_t batch_segments; /* most requests in one batch; 0 = 4096 */
+  uint32_t lanes;          /* batches in flight; 0 = 3 */
+  uint32_t timeout_ms;     /* device-side no-progress limit; 0 = 4000 */
+  uint32_t per_request;    /* 1: no batching. One request at a time through the plain sort (copy
+                              in, gqs_sort_<type>_dev, copy out, wait): the comparison baseline */
+  int32_t variant[3];      /* kernel variant per key type (GQS_U32, GQS_F32, GQS_F64); -1 = 0 */
+  uint32_t reserved[4];
+} gqs_server_config;
+
+typedef struct gqs_request_info {
+  uint32_t status;         /* gqs_status of the request */
+  uint32_t dtype;
+  uint64_t n;
+  uint64_t t_submit_ns;    /* gqs_srv_now_ns() clock */
+  uint64_t t_admit_ns;     /* keys resident on the device (copy enqueued) */
+  uint64_t t_launch_ns;    /* its batch launched */
+  uint64_t t_done_ns;      /* result in the output buffer */
+  uint32_t batch_requests; /* requests in its batch */
+  uint32_t lane;
+} gqs_request_info;
+
+typedef struct gqs_server_stats {
+  uint64_t submitted, completed, failed, completed_keys;
+  uint64_t batches, max_batch_requests;
+  uint64_t arena_bytes, arena_used, arena_peak;
+  uint64_t pending, outstanding;
+} gqs_server_stats;
+
+void gqs_srv_config_default(gqs_server_config* cfg);
+gqs_status gqs_srv_create(int device, const gqs_server_config* cfg, gqs_server** out);
+/* Finishes every submitted request, then stops the dispatcher and frees everything. */
+void gqs_srv_destroy(gqs_server* s);
+/* Queues a request: sort n keys of `dtype` read from `in` into `out` (host memory; may be the
+ * same buffer). Both stay owned by the caller and must stay valid until the request completes.
+ * n must be at most batch_keys. Returns at once with the request id. */
+gqs_status gqs_srv_submit(gqs_server* s, int dtype, const void* in, void* out, size_t n, uint64_t* id);
+/* Blocks until request `id` completes; returns its status, fills *info (may be NULL) and
+ * forgets the id. */
+gqs_status gqs_srv_wait(gqs_server* s, uint64_t id, gqs_request_info* info);
+/* Returns the next completed request not yet collected (completion order), or GQS_ERR_TIMEOUT
+ * when none completes within timeout_ms. */
+gqs_status gqs_srv_wait_any(gqs_server* s, uint64_t* id, gqs_request_info* info, uint32_t timeout_ms);
+/* Blocks until every submitted request has completed. */
+gqs_status gqs_srv_drain(gqs_server* s);
+gqs_status gqs_srv_stats(gqs_server* s, gqs_server_stats* out);
+/* The server's clock (steady, nanoseconds). */
+uint64_t gqs_srv_now_ns(void);
+
 /* Waits for the context's last enqueued sort and returns its device status. */
 gqs_status gqs_sync(gqs_ctx* ctx);
 

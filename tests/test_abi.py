@@ -43,3 +43,20 @@ def test_null_context_is_rejected():
     assert lib.gqs_sort_u32(None, None, None, 10) == 1
     assert lib.gqs_sort_u32_dev(None, None, None, 10, None) == 1
     assert lib.gqs_sync(None) == 1
+
+
+def test_batch_and_server_need_a_gb300():
+    """Without an sm_103 GPU the batch and server constructors fail with a status, not a crash."""
+    import torch
+    if torch.cuda.is_available():
+        import pytest
+        pytest.skip("a GPU is present")
+    lib = gqs_ctypes.load_library()
+    h = ctypes.c_void_p()
+    assert lib.gqs_batch_create(0, 0, 1000, 10, None, ctypes.byref(h)) == 6
+    assert lib.gqs_srv_create(0, None, ctypes.byref(h)) == 6
+    assert lib.gqs_batch_launch(None, 1, None) == 1
+    assert lib.gqs_srv_submit(None, 0, None, None, 1, ctypes.byref(ctypes.c_uint64())) == 1
+    cfg = gqs_ctypes.ServerConfig()
+    lib.gqs_srv_config_default(ctypes.byref(cfg))
+    assert cfg.budget_bytes == 64 << 30 and cfg.lanes == 3 and cfg.batch_segments == 4096
