@@ -181,9 +181,16 @@ struct Cfg {
   static constexpr int SLICE_KPL = sizeof(B) == 8 ? 8 : 16;
   static constexpr int SLICE = 32 * SLICE_KPL;
   static constexpr int LREC = 4 * TILE / TINY + 64;
+  // Local sort, first level: a sample split into up to NB_MAX buckets (mean TINY / 4 keys),
+  // used for tiles of at least SPLIT_MIN keys; SPLIT_SAMPLES keys are sorted to pick pivots.
+  static constexpr int NB_MAX = 256;
+  static constexpr int SPLIT_MIN = 8 * TINY;
+  static constexpr int SPLIT_SAMPLES = 256;
   static_assert(CHUNK % NC == 0, "chunk must be a multiple of the consumer threads");
   static_assert((CHUNK * sizeof(B)) % 16 == 0, "chunk must be a multiple of 16 bytes");
   static_assert(TILE > TINY, "tile must exceed the register sort");
+  static_assert(NB_MAX <= 256 && NB_MAX >= 32, "bucket labels are bytes; the scan takes 32..256 buckets");
+  static_assert(SPLIT_SAMPLES % 32 == 0 && SPLIT_SAMPLES >= NB_MAX, "samples per lane; one pivot per bucket");
 };
 
 struct Seg {
@@ -224,6 +231,12 @@ struct alignas(128) Smem {
   // local sort: segment records and their queue
   uint32_t lr_head, lr_tail, ls_done;
   LRec lrec[C::LREC];
+  // local sort, first level: pivots, bucket counts (then cursors), bucket starts, labels
+  typename C::B spl[C::NB_MAX];
+  uint32_t bcnt[C::NB_MAX];
+  uint32_t bstart[C::NB_MAX + 1];
+  uint32_t bnext;
+  uint8_t lb[C::TILE];
 };
 
 // ---------------------------------------------------------------------------
@@ -1075,6 +1088,93 @@ struct Persistent {
 #endif
   }
 
+  // First level of the on-chip sort for tiles of SPLIT_MIN keys or more: one multi-pivot
+  // partition of the whole tile. Warp 0 sorts SPLIT_SAMPLES evenly spaced keys in registers and
+  // keeps nb - 1 of them as pivots (nb a power of two, buckets of about TINY / 4 keys). Every
+  // consumer thread then labels its keys with their bucket (binary search over the pivots:
+  // bucket b holds pivot[b-1] < key <= pivot[b]) and counts them; after an exclusive scan of the
+  // counts a second pass scatters every key into B at its bucket's place. The buckets are
+  // disjoint ranges in final order: warps take them one at a time and sort each into A in
+  // registers, or publish one longer than TINY as a slice-partitioned segment. Whole CTA; returns
+  // the keys this warp finalised.
+  static __device__ __noinline__ uint32_t sample_split(const SortArgs<T>& a, Smem<C>& sm, B* A, uint32_t m,
+                                                       unsigned long long* lp) {
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    uint32_t nb = 2;
+    while (nb < (uint32_t)C::NB_MAX && nb * (uint32_t)(C::TINY / 4) < m) nb <<= 1;
+    for (uint32_t i = tid; i < nb; i += C::NC) sm.bcnt[i] = 0u;
+    if (warp == 0) {
+      constexpr int RS = C::SPLIT_SAMPLES / 32;
+      B v[RS];
+#pragma unroll
+      for (int r = 0; r < RS; ++r)
+        v[r] = A[(uint32_t)(((unsigned long long)(r * 32 + lane) * m) / (unsigned long long)C::SPLIT_SAMPLES)];
+      warp_bitonic<RS>(v);  // sample j is now v[j % RS] of lane j / RS
+      const uint32_t step = (uint32_t)C::SPLIT_SAMPLES / nb;
+#pragma unroll
+      for (int r = 0; r < RS; ++r) {
+        const uint32_t j = (uint32_t)lane * RS + r + 1u;
+        if (j % step == 0u && j / step < nb) sm.spl[j / step - 1u] = v[r];
+      }
+    }
+    cbar();
+    for (uint32_t i = tid; i < m; i += C::NC) {
+      const B k = A[i];
+      uint32_t b = 0;
+      for (uint32_t st = nb >> 1; st; st >>= 1) b += sm.spl[b + st - 1u] < k ? st : 0u;
+      sm.lb[i] = (uint8_t)b;
+      atomicAdd(&sm.bcnt[b], 1u);
+    }
+    cbar();
+    if (warp == 0) {  // exclusive scan of the counts: bucket starts, and cursors for the scatter
+      constexpr int PER = C::NB_MAX / 32;
+      const uint32_t per = nb > 32u ? nb / 32u : 1u;
+      uint32_t loc[PER];
+      uint32_t sum = 0;
+#pragma unroll
+      for (int q = 0; q < PER; ++q) {
+        const uint32_t idx = (uint32_t)lane * per + (uint32_t)q;
+        const uint32_t c = ((uint32_t)q < per && idx < nb) ? sm.bcnt[idx] : 0u;
+        loc[q] = sum;
+        sum += c;
+      }
+      uint32_t inc = sum;
+#pragma unroll
+      for (int d = 1; d < 32; d <<= 1) {
+        const uint32_t t = __shfl_up_sync(0xffffffffu, inc, d);
+        if (lane >= d) inc += t;
+      }
+      const uint32_t excl = inc - sum;
+#pragma unroll
+      for (int q = 0; q < PER; ++q) {
+        const uint32_t idx = (uint32_t)lane * per + (uint32_t)q;
+        if ((uint32_t)q < per && idx < nb) {
+          sm.bstart[idx] = excl + loc[q];
+          sm.bcnt[idx] = excl + loc[q];
+        }
+      }
+      if (lane == 0) {
+        sm.bstart[nb] = m;
+        sm.bnext = 0u;
+      }
+    }
+    cbar();
+    for (uint32_t i = tid; i < m; i += C::NC) {
+      const uint32_t pos = atomicAdd(&sm.bcnt[sm.lb[i]], 1u);
+      sm.tileB[pos] = A[i];
+    }
+    cbar();
+    uint32_t fin = 0;
+    for (;;) {
+      uint32_t b = 0;
+      if (lane == 0) b = atomicAdd(&sm.bnext, 1u);
+      b = __shfl_sync(0xffffffffu, b, 0);
+      if (b >= nb) break;
+      fin += place_child(a, sm, A, sm.bstart[b], sm.bstart[b + 1], 1u, lp);
+    }
+    return fin;
+  }
+
   // Sorts A[0, m) (comparison keys) with all consumer warps. On return A holds the keys sorted.
   static __device__ __noinline__ void local_sort(const SortArgs<T>& a, Smem<C>& sm, B* A, uint32_t m,
                                                  unsigned long long* lp) {
@@ -1089,7 +1189,10 @@ struct Persistent {
     }
     for (uint32_t i = tid; i < (uint32_t)C::LREC; i += C::NC) sm.lrec[i].seq = 0u;
     cbar();
-    if (warp == 0) {
+    if (m >= (uint32_t)C::SPLIT_MIN) {
+      const uint32_t fin = sample_split(a, sm, A, m, lp);
+      if (lane == 0 && fin) atomicAdd(&sm.ls_done, fin);
+    } else if (warp == 0) {
       const uint32_t fin = place_child(a, sm, A, 0, m, 0u, lp);
       if (lane == 0 && fin) atomicAdd(&sm.ls_done, fin);
     }
