@@ -235,7 +235,6 @@ struct alignas(128) Smem {
   typename C::B spl[C::NB_MAX];
   uint32_t bcnt[C::NB_MAX];
   uint32_t bstart[C::NB_MAX + 1];
-  uint32_t bnext;
   uint8_t lb[C::TILE];
 };
 
@@ -290,58 +289,78 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, Queue*
 // (Replaces the reference's work-group bitonic network, QuicksortKernels.cl:40-68.)
 // Flip form: each merge of size k starts by comparing e with its mirror e ^ (k-1), then
 // half-cleaners compare e with e ^ j; the lower index always keeps the minimum, so no
-// compare-exchange needs a per-element direction.
-template <int R, class K>
-__device__ __forceinline__ void warp_bitonic(K (&v)[R]) {
+// compare-exchange needs a per-element direction. N independent networks run interleaved,
+// which multiplies the independent work in every stage by N (the stages are a latency chain).
+template <int R, int N, class K>
+__device__ __forceinline__ void warp_bitonic_n(K (&v)[N * R]) {
   const int lane = threadIdx.x & 31;
 #pragma unroll
   for (int k = 2; k <= 32 * R; k <<= 1) {
     if (k <= R) {
 #pragma unroll
-      for (int r = 0; r < R; ++r) {
-        const int pr = r ^ (k - 1);
-        if (pr > r) {
-          const K a = v[r], b = v[pr];
-          v[r] = a < b ? a : b;
-          v[pr] = a < b ? b : a;
+      for (int n = 0; n < N; ++n)
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+          const int pr = r ^ (k - 1);
+          if (pr > r) {
+            const K a = v[n * R + r], b = v[n * R + pr];
+            v[n * R + r] = a < b ? a : b;
+            v[n * R + pr] = a < b ? b : a;
+          }
         }
-      }
     } else {
       const int lj = (k - 1) / R;
       const bool lower = (lane & (k / R / 2)) == 0;
-      K t[R];
+      K t[N * R];
 #pragma unroll
-      for (int r = 0; r < R; ++r) t[r] = __shfl_xor_sync(0xffffffffu, v[R - 1 - r], lj);
+      for (int n = 0; n < N; ++n)
 #pragma unroll
-      for (int r = 0; r < R; ++r) {
-        const K a = v[r], b = t[r];
-        v[r] = ((a > b) == lower) ? b : a;
-      }
+        for (int r = 0; r < R; ++r) t[n * R + r] = __shfl_xor_sync(0xffffffffu, v[n * R + R - 1 - r], lj);
+#pragma unroll
+      for (int n = 0; n < N; ++n)
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+          const K a = v[n * R + r], b = t[n * R + r];
+          v[n * R + r] = ((a > b) == lower) ? b : a;
+        }
     }
 #pragma unroll
     for (int j = k >> 2; j > 0; j >>= 1) {
       if (j < R) {
 #pragma unroll
-        for (int r = 0; r < R; ++r) {
-          const int pr = r ^ j;
-          if (pr > r) {
-            const K a = v[r], b = v[pr];
-            v[r] = a < b ? a : b;
-            v[pr] = a < b ? b : a;
+        for (int n = 0; n < N; ++n)
+#pragma unroll
+          for (int r = 0; r < R; ++r) {
+            const int pr = r ^ j;
+            if (pr > r) {
+              const K a = v[n * R + r], b = v[n * R + pr];
+              v[n * R + r] = a < b ? a : b;
+              v[n * R + pr] = a < b ? b : a;
+            }
           }
-        }
       } else {
         const int lj = j / R;
         const bool lower = (lane & lj) == 0;
+        K t[N * R];
 #pragma unroll
-        for (int r = 0; r < R; ++r) {
-          const K a = v[r];
-          const K b = __shfl_xor_sync(0xffffffffu, a, lj);
-          v[r] = ((a > b) == lower) ? b : a;
-        }
+        for (int n = 0; n < N; ++n)
+#pragma unroll
+          for (int r = 0; r < R; ++r) t[n * R + r] = __shfl_xor_sync(0xffffffffu, v[n * R + r], lj);
+#pragma unroll
+        for (int n = 0; n < N; ++n)
+#pragma unroll
+          for (int r = 0; r < R; ++r) {
+            const K a = v[n * R + r], b = t[n * R + r];
+            v[n * R + r] = ((a > b) == lower) ? b : a;
+          }
       }
     }
   }
+}
+
+template <int R, class K>
+__device__ __forceinline__ void warp_bitonic(K (&v)[R]) {
+  warp_bitonic_n<R, 1>(v);
 }
 
 template <class K>
@@ -1090,18 +1109,34 @@ struct Persistent {
 
   // First level of the on-chip sort for tiles of SPLIT_MIN keys or more: one multi-pivot
   // partition of the whole tile. Warp 0 sorts SPLIT_SAMPLES evenly spaced keys in registers and
-  // keeps nb - 1 of them as pivots (nb a power of two, buckets of about TINY / 4 keys). Every
-  // consumer thread then labels its keys with their bucket (binary search over the pivots:
-  // bucket b holds pivot[b-1] < key <= pivot[b]) and counts them; after an exclusive scan of the
-  // counts a second pass scatters every key into B at its bucket's place. The buckets are
-  // disjoint ranges in final order: warps take them one at a time and sort each into A in
-  // registers, or publish one longer than TINY as a slice-partitioned segment. Whole CTA; returns
-  // the keys this warp finalised.
-  static __device__ __noinline__ uint32_t sample_split(const SortArgs<T>& a, Smem<C>& sm, B* A, uint32_t m,
+  // keeps nb - 1 of them as pivots (nb a power of two, buckets of about TINY / 4 keys), stored as
+  // an implicit search tree in breadth-first order (node i has children 2i and 2i + 1), so the
+  // lanes of a warp reading one level of the tree hit distinct banks. Every consumer thread then
+  // labels its keys with their bucket (bucket b holds pivot[b-1] < key <= pivot[b]) and counts
+  // them; after an exclusive scan of the counts a second pass scatters every key into B at its
+  // bucket's place. The buckets are disjoint ranges in final order: each warp sorts its buckets
+  // into A in registers, or publishes one longer than TINY as a slice-partitioned segment. Whole
+  // CTA; returns the keys this warp finalised. (Inlined: as a called function its register
+  // demand made the kernel keep partition-loop values in local memory.)
+  static __device__ __forceinline__ uint32_t sample_split(const SortArgs<T>& a, Smem<C>& sm, B* A, uint32_t m,
                                                        unsigned long long* lp) {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    uint32_t nb = 2;
-    while (nb < (uint32_t)C::NB_MAX && nb * (uint32_t)(C::TINY / 4) < m) nb <<= 1;
+#ifdef GQS_PROFILE
+    long long tp = clock64();
+#define GQS_SPLIT_STAMP(k)                                             \
+  if (tid == 0) {                                                      \
+    const long long tn = clock64();                                    \
+    lp[k] += (unsigned long long)(tn - tp);                            \
+    tp = tn;                                                           \
+  }
+#else
+#define GQS_SPLIT_STAMP(k)
+#endif
+    uint32_t nb = 2, lg = 1;
+    while (nb < (uint32_t)C::NB_MAX && nb * (uint32_t)(C::TINY / 4) < m) {
+      nb <<= 1;
+      ++lg;
+    }
     for (uint32_t i = tid; i < nb; i += C::NC) sm.bcnt[i] = 0u;
     if (warp == 0) {
       constexpr int RS = C::SPLIT_SAMPLES / 32;
@@ -1110,22 +1145,30 @@ struct Persistent {
       for (int r = 0; r < RS; ++r)
         v[r] = A[(uint32_t)(((unsigned long long)(r * 32 + lane) * m) / (unsigned long long)C::SPLIT_SAMPLES)];
       warp_bitonic<RS>(v);  // sample j is now v[j % RS] of lane j / RS
-      const uint32_t step = (uint32_t)C::SPLIT_SAMPLES / nb;
+      B* smp = sm.tileB;    // free until the scatter
 #pragma unroll
-      for (int r = 0; r < RS; ++r) {
-        const uint32_t j = (uint32_t)lane * RS + r + 1u;
-        if (j % step == 0u && j / step < nb) sm.spl[j / step - 1u] = v[r];
+      for (int r = 0; r < RS; ++r) smp[lane * RS + r] = v[r];
+      __syncwarp();
+      // Tree node i (level l = floor(log2 i), p = i - 2^l) is pivot (2p + 1) * 2^(lg-l-1) - 1 in
+      // sorted order; pivot q is sample (q + 1) * (SPLIT_SAMPLES / nb) - 1.
+      const uint32_t step = (uint32_t)C::SPLIT_SAMPLES / nb;
+      for (uint32_t i = 1u + (uint32_t)lane; i < nb; i += 32u) {
+        const uint32_t l = 31u - (uint32_t)__clz(i);
+        const uint32_t q = ((2u * (i - (1u << l)) + 1u) << (lg - l - 1u)) - 1u;
+        sm.spl[i] = smp[(q + 1u) * step - 1u];
       }
     }
     cbar();
+    GQS_SPLIT_STAMP(9)
     for (uint32_t i = tid; i < m; i += C::NC) {
       const B k = A[i];
-      uint32_t b = 0;
-      for (uint32_t st = nb >> 1; st; st >>= 1) b += sm.spl[b + st - 1u] < k ? st : 0u;
-      sm.lb[i] = (uint8_t)b;
-      atomicAdd(&sm.bcnt[b], 1u);
+      uint32_t b = 1u;
+      for (uint32_t l = 0; l < lg; ++l) b = 2u * b + (sm.spl[b] < k ? 1u : 0u);
+      sm.lb[i] = (uint8_t)(b - nb);
+      atomicAdd(&sm.bcnt[b - nb], 1u);
     }
     cbar();
+    GQS_SPLIT_STAMP(10)
     if (warp == 0) {  // exclusive scan of the counts: bucket starts, and cursors for the scatter
       constexpr int PER = C::NB_MAX / 32;
       const uint32_t per = nb > 32u ? nb / 32u : 1u;
@@ -1153,30 +1196,27 @@ struct Persistent {
           sm.bcnt[idx] = excl + loc[q];
         }
       }
-      if (lane == 0) {
-        sm.bstart[nb] = m;
-        sm.bnext = 0u;
-      }
+      if (lane == 0) sm.bstart[nb] = m;
     }
     cbar();
+    GQS_SPLIT_STAMP(11)
     for (uint32_t i = tid; i < m; i += C::NC) {
       const uint32_t pos = atomicAdd(&sm.bcnt[sm.lb[i]], 1u);
       sm.tileB[pos] = A[i];
     }
     cbar();
+    GQS_SPLIT_STAMP(12)
     uint32_t fin = 0;
-    for (;;) {
-      uint32_t b = 0;
-      if (lane == 0) b = atomicAdd(&sm.bnext, 1u);
-      b = __shfl_sync(0xffffffffu, b, 0);
-      if (b >= nb) break;
+    // warp w takes buckets w, w + NCW, w + 2 NCW, ...
+    for (uint32_t b = (uint32_t)warp; b < nb; b += (uint32_t)C::NCW)
       fin += place_child(a, sm, A, sm.bstart[b], sm.bstart[b + 1], 1u, lp);
-    }
+    GQS_SPLIT_STAMP(13)
+#undef GQS_SPLIT_STAMP
     return fin;
   }
 
   // Sorts A[0, m) (comparison keys) with all consumer warps. On return A holds the keys sorted.
-  static __device__ __noinline__ void local_sort(const SortArgs<T>& a, Smem<C>& sm, B* A, uint32_t m,
+  static __device__ __forceinline__ void local_sort(const SortArgs<T>& a, Smem<C>& sm, B* A, uint32_t m,
                                                  unsigned long long* lp) {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 #ifdef GQS_PROFILE
