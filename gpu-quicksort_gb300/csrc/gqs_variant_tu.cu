@@ -20,14 +20,14 @@ struct Pick;
   template <>                                                                         \
   struct Pick<V> {                                                                    \
     using C = Cfg<T, NCW, TILE, CHUNK, STAGES, R, WM>;                                \
-    static constexpr const char* name = #S "_ncw" #NCW "_tile" #TILE "_chunk" #CHUNK "_st" #STAGES; \
+    static const char* name() { return #S "_ncw" #NCW "_tile" #TILE "_chunk" #CHUNK "_st" #STAGES; } \
   };
 GQS_TU_LIST(GQS_PICK)
 #undef GQS_PICK
 using Chosen = Pick<GQS_TU_INDEX>;
 }  // namespace
 
-VariantInfo GQS_FN(info_)() { return VariantOps<Chosen::C>::info(Chosen::name); }
+VariantInfo GQS_FN(info_)() { return VariantOps<Chosen::C>::info(Chosen::name()); }
 int GQS_FN(prepare_)() { return VariantOps<Chosen::C>::prepare(); }
 cudaError_t GQS_FN(launch_)(const LaunchParams& p) { return VariantOps<Chosen::C>::launch(p); }
 
