@@ -29,6 +29,7 @@ VARIANT_TU = "gqs_variant_tu.cu"  # compiled once per (key type, variant index)
 LIB = os.path.join(HERE, "libgqs.so")
 PROF_LIB = os.path.join(HERE, "libgqs_prof.so")  # -DGQS_PROFILE: per-role cycle counters
 WORKLOAD_LIB = os.path.join(HERE, "libgqs_workload.so")
+CLI = os.path.join(HERE, "quicksort")  # the reference-compatible benchmark command line
 
 
 def _nvcc() -> str:
@@ -108,9 +109,16 @@ def build(force: bool = False, verbose: bool = False, profile: bool = False) -> 
             f.result()
     if force or jobs or _stale(lib, objs):
         _run([nvcc] + ARCH + ["-shared", "-o", lib] + objs + ["-Xcompiler", "-fPIC"])
+    out = {"lib": lib, "workload": WORKLOAD_LIB}
+    csrc = os.path.join(HERE, "cli", "quicksort_main.cpp")
+    if not profile and os.path.exists(csrc):
+        if force or _stale(CLI, [csrc, LIB, WORKLOAD_LIB, os.path.join(INCLUDE, "gqs.h")]):
+            _run([nvcc, "-O2", "-std=c++17", "-I" + INCLUDE, "-I" + os.path.join(HERE, "workload"), csrc,
+                  "-L" + HERE, "-lgqs", "-lgqs_workload", "-Xlinker", "-rpath,$ORIGIN", "-o", CLI])
+        out["cli"] = CLI
     if verbose:
-        print("built", lib, WORKLOAD_LIB)
-    return {"lib": lib, "workload": WORKLOAD_LIB}
+        print("built", lib, WORKLOAD_LIB, out.get("cli", ""))
+    return out
 
 
 if __name__ == "__main__":

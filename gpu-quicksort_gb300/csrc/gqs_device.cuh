@@ -253,20 +253,27 @@ __device__ __forceinline__ unsigned long long progress_word(Queue* q) {
 // A wait that gives up (and records a timeout) only when the whole sort has made no
 // progress for `timeout_ns`, or when another CTA has already recorded an error.
 struct Waiter {
-  unsigned long long t0, last;
+  // The shared progress counters are sampled at most every kPollNs (the SM-local global timer
+  // is read in between), so waiting warps do not flood the queue's hot cache lines.
+  static constexpr unsigned long long kPollNs = 20000;
+  unsigned long long t0, tcheck, last;
   uint32_t spins;
-  __device__ __forceinline__ explicit Waiter(Queue* q) : t0(global_timer_ns()), last(progress_word(q)), spins(0) {}
+  __device__ __forceinline__ explicit Waiter(Queue*) : t0(global_timer_ns()), tcheck(t0), last(~0ull), spins(0) {}
   __device__ __forceinline__ bool step(Queue* q, unsigned long long timeout_ns, uint32_t where, bool sleep) {
     ++spins;
-    if ((spins & 31u) == 0u) {
-      if (ld_relaxed(&q->error)) return false;
-      unsigned long long p = progress_word(q), now = global_timer_ns();
-      if (p != last) {
-        last = p;
-        t0 = now;
-      } else if (now - t0 > timeout_ns) {
-        set_error(q, ST_TIMEOUT, where);
-        return false;
+    if ((spins & 15u) == 0u) {
+      const unsigned long long now = global_timer_ns();
+      if (now - tcheck >= kPollNs) {
+        tcheck = now;
+        if (ld_relaxed(&q->error)) return false;
+        const unsigned long long p = progress_word(q);
+        if (p != last) {
+          last = p;
+          t0 = now;
+        } else if (now - t0 > timeout_ns) {
+          set_error(q, ST_TIMEOUT, where);
+          return false;
+        }
       }
     }
     if (sleep) __nanosleep(spins < 64 ? 64 : 512);
@@ -584,12 +591,16 @@ struct Persistent {
   // Stage src[cs, ce) into shared memory at `dst`, rounded out to whole 16-byte granules of
   // global memory (a granule never straddles a page, so the rounding cannot fault; the extra
   // bytes are never read). Returns the element offset of src[cs] inside `dst`.
+  // The keys were written with plain stores by other warps and CTAs, made visible to this
+  // thread by the acquire of the job's ticket; the global proxy fence extends that to the bulk
+  // copy, which reads through the async proxy.
   static __device__ __forceinline__ uint32_t stage_range(const B* src, unsigned long long cs,
                                                          unsigned long long ce, B* dst, uint64_t* bar) {
     const uintptr_t lo = reinterpret_cast<uintptr_t>(src + cs);
     const uintptr_t ga = lo & ~uintptr_t(15);
     const uintptr_t gb = (reinterpret_cast<uintptr_t>(src + ce) + 15) & ~uintptr_t(15);
     const uint32_t bytes = (uint32_t)(gb - ga);
+    fence_proxy_async_global();
     fence_proxy_async_smem();
     mbar_arrive_expect_tx(bar, bytes);
     bulk_load(dst, reinterpret_cast<const void*>(ga), bytes, bar);

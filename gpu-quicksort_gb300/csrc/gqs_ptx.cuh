@@ -55,6 +55,11 @@ __device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wa
 __device__ __forceinline__ void fence_proxy_async_smem() {
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
+// The same for global memory: after an acquire has made other threads' plain stores visible to
+// this thread, this fence makes its later bulk (async-proxy) loads see them too.
+__device__ __forceinline__ void fence_proxy_async_global() {
+  asm volatile("fence.proxy.async.global;" ::: "memory");
+}
 
 // ---- global memory with explicit scope ------------------------------------
 __device__ __forceinline__ uint32_t ld_acquire(const uint32_t* p) {

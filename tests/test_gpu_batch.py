@@ -10,10 +10,10 @@ pytestmark = pytest.mark.gpu
 DIST = {"u32": "uniform", "f32": "gaussian", "f64": "uniform"}
 
 
-def check_segments(a, b, off):
+def check_segments(a, b, off, what=None):
     for i in range(len(off) - 1):
         s, e = int(off[i]), int(off[i + 1])
-        assert np.array_equal(b[s:e], np.sort(a[s:e])), (i, s, e)
+        assert np.array_equal(b[s:e], np.sort(a[s:e])), (what, i, s, e)
 
 
 def run_batch(batch, a, off):
@@ -61,7 +61,7 @@ def test_every_variant_in_a_batch(dtype):
             batch.set_variant(v)
             b, st = run_batch(batch, a, off)
             assert st["variant"] == v
-            check_segments(a, b, off)
+            check_segments(a, b, off, f"variant {v}")
 
 
 @pytest.mark.parametrize("dtype", ["u32", "f64"])
