@@ -380,7 +380,9 @@ gqs_status gqs_reserve(gqs_ctx* c, int dtype, size_t n, size_t nseg, int with_bu
     c->blocks_per_sm[dtype][v] = gqs::variant_prepare(dtype, v);
     if (!c->blocks_per_sm[dtype][v]) return GQS_ERR_NO_DEVICE;
   }
+  if (n >= (1ull << 40) || nseg >= (1ull << 31)) return GQS_ERR_INVALID;
   const size_t cap = job_capacity(vi, n, nseg ? nseg : 1);
+  if (cap >= (1ull << 32) || ticket_ring(vi, n, nseg ? nseg : 1) > (1ull << 31)) return GQS_ERR_INVALID;
   if (c->job_cap < cap) {
     void* p = c->jobs;
     size_t bytes = c->job_cap * sizeof(gqs::Job);
@@ -446,6 +448,78 @@ gqs_status gqs_sort_segments_f32(gqs_ctx* c, float* k, size_t n, const uint64_t*
 }
 gqs_status gqs_sort_segments_f64(gqs_ctx* c, double* k, size_t n, const uint64_t* o, size_t ns) {
   return sort_segments_host(c, gqs::DT_F64, k, n, o, ns);
+}
+
+gqs_status gqs_selftest_stalled_queue(gqs_ctx* c, int dtype, uint32_t timeout_ms) {
+  if (!c || dtype < 0 || dtype > 2) return GQS_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(c->mu);
+  DeviceGuard dg(c->device);
+  (void)wait_pending_locked(c);
+  const int v = c->variant[dtype];
+  const gqs::VariantInfo vi = gqs::variant_info(dtype, v);
+  if (!c->blocks_per_sm[dtype][v]) {
+    c->blocks_per_sm[dtype][v] = gqs::variant_prepare(dtype, v);
+    if (!c->blocks_per_sm[dtype][v]) return GQS_ERR_NO_DEVICE;
+  }
+  const size_t n = 1024;  // pools for a small sort; the kernel touches none of the keys
+  const size_t cap = job_capacity(vi, n, 1), ring = ticket_ring(vi, n, 1);
+  gqs_status st = GQS_OK;
+  if (c->job_cap < cap) {
+    void* p = c->jobs;
+    size_t bytes = c->job_cap * sizeof(gqs::Job);
+    st = grow(&p, &bytes, cap * sizeof(gqs::Job));
+    c->jobs = static_cast<gqs::Job*>(p);
+    c->job_cap = c->jobs ? bytes / sizeof(gqs::Job) : 0;
+    if (st != GQS_OK) return st;
+  }
+  if (c->tmap_len < ring) {
+    void* p = c->tmap;
+    size_t bytes = c->tmap_len * sizeof(unsigned long long);
+    st = grow(&p, &bytes, ring * sizeof(unsigned long long));
+    c->tmap = static_cast<unsigned long long*>(p);
+    c->tmap_len = c->tmap ? ring : 0;
+    if (st != GQS_OK) return st;
+  }
+  if ((st = grow(&c->pool_dn, &c->pool_dn_bytes, n * kElemSize[dtype])) != GQS_OK) return st;
+  void* po = c->offs;
+  st = grow(&po, &c->offs_cap, 4 * sizeof(uint64_t));
+  c->offs = static_cast<unsigned long long*>(po);
+  if (st != GQS_OK) return st;
+  // The queue claims one key (total = 1) while the segment count is zero: no job is ever seeded,
+  // so done never reaches total and every wait runs into its limit.
+  std::memset(c->q_host, 0, sizeof(gqs::Queue));
+  c->q_host->total = 1;
+  cudaError_t e = cudaMemcpyAsync(c->q, c->q_host, sizeof(gqs::Queue), cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(c->offs, 0, 4 * sizeof(uint64_t), c->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(c->tmap, 0, ring * sizeof(unsigned long long), c->stream);
+  if (e != cudaSuccess) return cuda_status(e);
+  gqs::LaunchParams p{};
+  p.d = c->pool_dn;
+  p.dn = c->pool_dn;
+  p.jobs = c->jobs;
+  p.q = c->q;
+  p.tmap = c->tmap;
+  p.capacity = (uint32_t)c->job_cap;
+  p.tmask = (uint32_t)(ring - 1);
+  p.timeout_ns = (unsigned long long)(timeout_ms ? timeout_ms : (c->cfg.timeout_ms ? c->cfg.timeout_ms : 4000)) *
+                 1000000ull;
+  p.offsets = c->offs + 1;
+  p.nseg_dev = c->offs;  // zero segments
+  p.nseg = 1;
+  p.n = n;
+  p.variant = v;
+  p.grid = c->num_sms * c->blocks_per_sm[dtype][v];
+  p.stream = c->stream;
+  e = gqs::launch_sort(dtype, p);
+  if (e == cudaSuccess) e = cudaEventRecord(c->ev_done, c->stream);
+  if (e != cudaSuccess) return cuda_status(e);
+  c->pending = true;
+  c->pending_timed = false;
+  c->pending_dtype = dtype;
+  c->pending_variant = v;
+  c->pending_grid = p.grid;
+  c->pending_keys = 0;
+  return wait_pending_locked(c);
 }
 
 gqs_status gqs_sync(gqs_ctx* c) {
@@ -514,6 +588,7 @@ const char* gqs_strerror(gqs_status s) {
     case GQS_ERR_CAPACITY: return "device job queue overflow";
     case GQS_ERR_NO_DEVICE: return "no sm_103 CUDA device";
     case GQS_ERR_INTERNAL: return "internal error";
+    case GQS_ERR_CANCELLED: return "request cancelled";
   }
   return "unknown status";
 }

@@ -178,8 +178,8 @@ void complete_locked(gqs_server* s, Req* r, gqs_status st) {
   s->completed.push_back(r->id);
   --s->outstanding;
   ++s->stats.completed;
-  s->stats.completed_keys += r->n;
-  if (st != GQS_OK) ++s->stats.failed;
+  if (st == GQS_OK) s->stats.completed_keys += r->n;
+  if (st != GQS_OK && st != GQS_ERR_CANCELLED) ++s->stats.failed;
 }
 
 // Dispatcher: retire finished lanes. Lock held.
@@ -628,6 +628,39 @@ gqs_status gqs_srv_wait_any(gqs_server* s, uint64_t* id, gqs_request_info* info,
     if (s->cv_done.wait_until(lk, deadline) == std::cv_status::timeout && s->completed.empty())
       return GQS_ERR_TIMEOUT;
   }
+}
+
+gqs_status gqs_srv_cancel(gqs_server* s, uint64_t id) {
+  if (!s) return GQS_ERR_INVALID;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->reqs.find(id);
+    if (it == s->reqs.end() || it->second->done) return GQS_ERR_INVALID;
+    Req* r = it->second.get();
+    auto pit = std::find(s->pending.begin(), s->pending.end(), r);
+    if (pit != s->pending.end()) {
+      s->pending.erase(pit);
+    } else {
+      std::deque<Req*>& q = s->admitted[r->dtype];
+      auto ait = std::find(q.begin(), q.end(), r);
+      if (ait == q.end()) return GQS_ERR_INVALID;  // already on the GPU
+      q.erase(ait);
+      // its keys may still be on the way in; later copies into this space are ordered after
+      // it on the same copy stream
+      s->arena.release(r->off, r->n * gqs::kElemSize[r->dtype]);
+      auto rd = s->rounds.find(r->round);
+      if (rd != s->rounds.end() && --rd->second.refs == 0) {
+        cudaEventDestroy(rd->second.ev);
+        s->rounds.erase(rd);
+      }
+      s->stats.arena_used = s->arena.used();
+    }
+    complete_locked(s, r, GQS_ERR_CANCELLED);
+    ++s->stats.cancelled;
+  }
+  s->cv_done.notify_all();
+  s->cv_work.notify_one();
+  return GQS_OK;
 }
 
 gqs_status gqs_srv_drain(gqs_server* s) {

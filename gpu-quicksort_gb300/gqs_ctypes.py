@@ -21,7 +21,7 @@ DIST = {"uniform": 0, "sorted": 1, "reverse": 2, "distinct16": 3, "zipf": 4, "ga
         "allequal": 7}
 
 STATUS = {0: "GQS_OK", 1: "GQS_ERR_INVALID", 2: "GQS_ERR_CUDA", 3: "GQS_ERR_NOMEM", 4: "GQS_ERR_TIMEOUT",
-          5: "GQS_ERR_CAPACITY", 6: "GQS_ERR_NO_DEVICE", 7: "GQS_ERR_INTERNAL"}
+          5: "GQS_ERR_CAPACITY", 6: "GQS_ERR_NO_DEVICE", 7: "GQS_ERR_INTERNAL", 8: "GQS_ERR_CANCELLED"}
 
 # Every function include/gqs.h declares.
 EXPORTS = [
@@ -35,7 +35,8 @@ EXPORTS = [
     "gqs_batch_create", "gqs_batch_destroy", "gqs_batch_keys", "gqs_batch_offsets", "gqs_batch_launch",
     "gqs_batch_wait", "gqs_batch_copy_in", "gqs_batch_copy_out", "gqs_batch_set_variant", "gqs_batch_get_variant", "gqs_batch_autotune",
     "gqs_srv_config_default", "gqs_srv_create", "gqs_srv_destroy", "gqs_srv_submit", "gqs_srv_wait",
-    "gqs_srv_wait_any", "gqs_srv_drain", "gqs_srv_stats", "gqs_srv_now_ns",
+    "gqs_srv_wait_any", "gqs_srv_cancel", "gqs_srv_drain", "gqs_srv_stats", "gqs_srv_now_ns",
+    "gqs_selftest_stalled_queue",
 ]
 
 
@@ -83,7 +84,7 @@ class RequestInfo(C.Structure):
 
 
 class ServerStats(C.Structure):
-    _fields_ = [(k, C.c_uint64) for k in ("submitted", "completed", "failed", "completed_keys", "batches",
+    _fields_ = [(k, C.c_uint64) for k in ("submitted", "completed", "failed", "cancelled", "completed_keys", "batches",
                                           "max_batch_requests", "arena_bytes", "arena_used", "arena_peak",
                                           "pending", "outstanding")]
 
@@ -181,6 +182,10 @@ def load_library(path: str | None = None) -> C.CDLL:
     lib.gqs_srv_wait.restype = st
     lib.gqs_srv_wait_any.argtypes = [vp, C.POINTER(C.c_uint64), C.POINTER(RequestInfo), C.c_uint32]
     lib.gqs_srv_wait_any.restype = st
+    lib.gqs_srv_cancel.argtypes = [vp, C.c_uint64]
+    lib.gqs_srv_cancel.restype = st
+    lib.gqs_selftest_stalled_queue.argtypes = [vp, C.c_int, C.c_uint32]
+    lib.gqs_selftest_stalled_queue.restype = st
     lib.gqs_srv_drain.argtypes = [vp]
     lib.gqs_srv_drain.restype = st
     lib.gqs_srv_stats.argtypes = [vp, C.POINTER(ServerStats)]
@@ -281,6 +286,10 @@ class Context:
 
     def set_variant(self, dtype: str, v: int) -> None:
         _check(self.lib.gqs_set_variant(self.h, DTYPES[dtype], v), "gqs_set_variant")
+
+    def selftest_stalled_queue(self, dtype: str, timeout_ms: int) -> int:
+        """Runs the kernel on a queue that can never finish; returns the status it reports."""
+        return self.lib.gqs_selftest_stalled_queue(self.h, DTYPES[dtype], timeout_ms)
 
     def get_variant(self, dtype: str) -> int:
         return self.lib.gqs_get_variant(self.h, DTYPES[dtype])
@@ -429,6 +438,9 @@ class Server:
         info = RequestInfo()
         code = self.lib.gqs_srv_wait_any(self.h, C.byref(rid), C.byref(info), timeout_ms)
         return code, rid.value, info.as_dict()
+
+    def cancel(self, rid: int) -> int:
+        return self.lib.gqs_srv_cancel(self.h, rid)
 
     def drain(self) -> int:
         return self.lib.gqs_srv_drain(self.h)

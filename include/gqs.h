@@ -40,7 +40,8 @@ typedef enum gqs_status {
   GQS_ERR_TIMEOUT = 4,   /* a bounded device-side wait ran out (the sort made no progress) */
   GQS_ERR_CAPACITY = 5,  /* the device job queue overflowed (pathological pivot sequence) */
   GQS_ERR_NO_DEVICE = 6, /* no usable CUDA device, or not an sm_103 GPU */
-  GQS_ERR_INTERNAL = 7   /* an internal invariant failed on the device */
+  GQS_ERR_INTERNAL = 7,  /* an internal invariant failed on the device */
+  GQS_ERR_CANCELLED = 8  /* a server request was cancelled before it ran */
 } gqs_status;
 
 typedef enum gqs_dtype { GQS_U32 = 0, GQS_F32 = 1, GQS_F64 = 2 } gqs_dtype;
@@ -217,7 +218,7 @@ typedef struct gqs_request_info {
 } gqs_request_info;
 
 typedef struct gqs_server_stats {
-  uint64_t submitted, completed, failed, completed_keys;
+  uint64_t submitted, completed, failed, cancelled, completed_keys;
   uint64_t batches, max_batch_requests;
   uint64_t arena_bytes, arena_used, arena_peak;
   uint64_t pending, outstanding;
@@ -237,11 +238,23 @@ gqs_status gqs_srv_wait(gqs_server* s, uint64_t id, gqs_request_info* info);
 /* Returns the next completed request not yet collected (completion order), or GQS_ERR_TIMEOUT
  * when none completes within timeout_ms. */
 gqs_status gqs_srv_wait_any(gqs_server* s, uint64_t* id, gqs_request_info* info, uint32_t timeout_ms);
+/* Cancels a request that has not started: it completes at once with GQS_ERR_CANCELLED and its
+ * device memory is released. Returns GQS_OK if it was cancelled, GQS_ERR_INVALID if the id is
+ * unknown or the request is already running or finished. */
+gqs_status gqs_srv_cancel(gqs_server* s, uint64_t id);
 /* Blocks until every submitted request has completed. */
 gqs_status gqs_srv_drain(gqs_server* s);
 gqs_status gqs_srv_stats(gqs_server* s, gqs_server_stats* out);
 /* The server's clock (steady, nanoseconds). */
 uint64_t gqs_srv_now_ns(void);
+
+/* Self-test of the bounded device waits. Runs the persistent kernel (key type `dtype`) on a job
+ * queue that claims one unsorted key but holds no work, so every role of the kernel waits for
+ * progress that never comes. Returns the status the kernel reports: GQS_ERR_TIMEOUT after about
+ * timeout_ms (0 means the context's timeout) when the waits end as designed. No GPU fault, trap
+ * or hang is involved; the context stays usable. No reference counterpart (the reference waits
+ * on the host with blocking reads). */
+gqs_status gqs_selftest_stalled_queue(gqs_ctx* ctx, int dtype, uint32_t timeout_ms);
 
 /* Waits for the context's last enqueued sort and returns its device status. */
 gqs_status gqs_sync(gqs_ctx* ctx);
