@@ -67,6 +67,17 @@ def dist_env():
     return rank, world, local
 
 
+def max_over_ranks(x, dist):
+    """The largest value of x over all ranks; x itself without a process group."""
+    if dist is None:
+        return x
+    import torch
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def workload_name(args, n):
     if args.config == "batched":
         return f"batched segmented sort: 4096 uint32 arrays, lengths log-uniform in [32, 2^20], {n} keys"
@@ -161,10 +172,18 @@ def cpu_baseline(args, n_full):
     t1 = time.perf_counter()
     oracle_ctypes.std_sort(c)
     t_std = time.perf_counter() - t1
+    # the reference's own CPU quicksort<T> (GPU-Quicksort_Full_SYCL/QuicksortMain.cpp:213-259,
+    # unused by its driver), restated in the oracle, one core
+    d = a[:ns1].copy()
+    t2 = time.perf_counter()
+    oracle_ctypes.cpu_quicksort(d)
+    t_q = time.perf_counter() - t2
     return {"value": ns / t / 1e9, "unit": "Gkeys/s", "cores": threads, "kind": "port",
             "sample": f"GPUQSort<T> restatement (oracle/gqs_oracle.cpp) on {ns} {args.dtype} keys of the same "
                       f"distribution, {threads} threads, one sort of {t:.3f} s",
             "std_sort_1core": {"value": ns1 / t_std / 1e9, "unit": "Gkeys/s", "keys": ns1},
+            "reference_cpu_quicksort_1core": {"value": ns1 / t_q / 1e9, "unit": "Gkeys/s", "keys": ns1,
+                                              "bit_exact_vs_std_sort": bool(np.array_equal(c, d))},
             "cpu": platform.processor() or platform.machine()}
 
 
@@ -445,7 +464,7 @@ def run_batched(args, gqs_ctypes, rank, local, world, dist, barrier):
     torch.cuda.synchronize()
     barrier()
     clk = clocks.stop()
-    t = sum(a.elapsed_time(b) for a, b in zip(ev0, ev1)) / 1e3
+    t = max_over_ranks(sum(a.elapsed_time(b) for a, b in zip(ev0, ev1)) / 1e3, dist)
     value = n * world * args.steps / t / 1e9
     # end to end through the public batch calls: pinned host -> arena, replay, arena -> host
     out = torch.empty_like(host_in, pin_memory=True)
@@ -459,8 +478,9 @@ def run_batched(args, gqs_ctypes, rank, local, world, dist, barrier):
         batch.copy_out(ov)
         if i:
             times.append(time.perf_counter() - t0)
-    e2e = {"value": n * args.steps / sum(times) / 1e9, "unit": "Gkeys/s", "h2d_bytes_per_step": n * esize,
-           "d2h_bytes_per_step": n * esize, "ms_per_step": 1e3 * sum(times) / args.steps,
+    tsum = max_over_ranks(sum(times), dist)
+    e2e = {"value": n * world * args.steps / tsum / 1e9, "unit": "Gkeys/s", "h2d_bytes_per_step": n * esize,
+           "d2h_bytes_per_step": n * esize, "ms_per_step": 1e3 * tsum / args.steps,
            "api": "gqs_batch_copy_in + gqs_batch_launch + gqs_batch_wait + gqs_batch_copy_out (pinned)"}
     # the same arrays sorted by one plain call each (device pointers, enqueued back to back)
     ctx = gqs_ctypes.Context(device=local, sync=False, timing=False, variant=0)
@@ -627,11 +647,7 @@ def main():
     wall = time.perf_counter() - wall0
     clk = clocks.stop()
     step_ms = [a.elapsed_time(b) for a, b in zip(ev0, ev1)]
-    t_sort = sum(step_ms) / 1e3
-    if dist is not None:
-        tt = torch.tensor([t_sort], dtype=torch.float64, device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_sort = float(tt.item())
+    t_sort = max_over_ranks(sum(step_ms) / 1e3, dist)
     value = n * world * args.steps / t_sort / 1e9
 
     # ---- end to end through the host-pointer call
@@ -648,11 +664,7 @@ def main():
             t0 = time.perf_counter()
             ctx.sort(wv)
             times.append(time.perf_counter() - t0)
-        tsum = sum(times)
-        if dist is not None:
-            tt = torch.tensor([tsum], dtype=torch.float64, device="cuda")
-            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-            tsum = float(tt.item())
+        tsum = max_over_ranks(sum(times), dist)
         e2e = {"value": n * world * args.steps / tsum / 1e9, "unit": "Gkeys/s",
                "h2d_bytes_per_step": n * esize, "d2h_bytes_per_step": n * esize,
                "ms_per_step": 1e3 * tsum / args.steps, "api": "gqs_sort_" + args.dtype + " (host pointers, pinned)"}
