@@ -44,7 +44,7 @@ def parse():
     p.add_argument("--steps", type=int, default=5)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--config", default="plain", choices=["plain", "batched", "tiles", "serve"])
+    p.add_argument("--config", default="plain", choices=["plain", "batched", "tiles", "serve", "pairs"])
     p.add_argument("--dtype", default="u32", choices=["u32", "f32", "f64"])
     p.add_argument("--dist", default="uniform")
     p.add_argument("--log2n", type=int, default=28)
@@ -405,6 +405,66 @@ def run_serve(args, gqs_ctypes):
     }
 
 
+def run_pairs(args, gqs_ctypes, rank, local, world, dist, barrier):
+    """Key-value sort: 2^log2n u32 (or f32) keys, each carrying its uint32 index."""
+    import torch
+    n = 1 << args.log2n
+    dtype = args.dtype if args.dtype in ("u32", "f32") else "u32"
+    keys = gqs_ctypes.generate(dtype, args.dist if dtype == "u32" else "gaussian", SEED + rank, n)
+    kp = torch.from_numpy(keys.view(np.int32)).cuda()
+    vp = torch.arange(n, dtype=torch.int32, device="cuda")
+    k, v = torch.empty_like(kp), torch.empty_like(vp)
+    ctx = gqs_ctypes.Context(device=local, sync=False, timing=True)
+    stream = torch.cuda.current_stream()
+
+    def step():
+        rc = ctx.sort_pairs_dev(dtype, k.data_ptr(), v.data_ptr(), n, stream.cuda_stream)
+        if rc != 0:
+            raise RuntimeError(f"pair sort failed: {gqs_ctypes.STATUS.get(rc, rc)}")
+
+    for _ in range(args.warmup):
+        k.copy_(kp)
+        v.copy_(vp)
+        step()
+        if ctx.stats()["status"] != 0:
+            raise RuntimeError("pair sort failed")
+    order = torch.sort(kp.to(torch.int64) & 0xFFFFFFFF if dtype == "u32" else kp.view(torch.float32),
+                       stable=True).indices
+    check = {"stable_argsort_equal_to_torch": bool(torch.equal(v.to(torch.int64), order))}
+    ev0 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ev1 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    kms = []
+    barrier()
+    for i in range(args.steps):
+        k.copy_(kp)
+        v.copy_(vp)
+        ev0[i].record(stream)
+        step()
+        ev1[i].record(stream)
+        st = ctx.stats()
+        kms.append(st["kernel_ms"])
+    torch.cuda.synchronize()
+    barrier()
+    t = max_over_ranks(sum(a.elapsed_time(b) for a, b in zip(ev0, ev1)) / 1e3, dist)
+    ctx.close()
+    if rank != 0:
+        return None
+    peak, peak_src = measured_peak()
+    km = float(np.mean(kms))
+    ab = float(st["algo_bytes"])
+    return {"metric": f"Gpairs/s (key-value sort, 2^{args.log2n} {dtype} keys + uint32 values)",
+            "value": n * world * args.steps / t / 1e9, "unit": "Gpairs/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": f"{dtype} keys + u32 values (packed u64 words)",
+            "data": "synthetic (seeded generator, gpu-quicksort_gb300/workload)",
+            "config": {"workload": f"key-value sort of 2^{args.log2n} pairs", "keys": n,
+                       "l2": "inputs larger than L2 (rewritten from pristine copies before every step)"},
+            "roofline": {"bound": "hbm", "achieved": ab / (km / 1e3) / 1e9, "peak": peak, "unit": "GB/s",
+                         "frac": ab / (km / 1e3) / 1e9 / peak, "kernel": "gqs::persistent_kernel (u64 words)",
+                         "kernel_ms": km, "algo_bytes_per_launch": ab, "peak_source": peak_src},
+            "check": check, "gpu_launches": 4 * args.steps}
+
+
 def run_batched(args, gqs_ctypes, rank, local, world, dist, barrier):
     """4096 uint32 arrays, lengths log-uniform in [32, 2^20], as one graph-captured batch."""
     import torch
@@ -546,8 +606,9 @@ def main():
         if dist is not None:
             dist.barrier()
 
-    if args.config == "batched":
-        line = run_batched(args, gqs_ctypes, rank, local, world, dist, barrier)
+    if args.config in ("batched", "pairs"):
+        runner = run_batched if args.config == "batched" else run_pairs
+        line = runner(args, gqs_ctypes, rank, local, world, dist, barrier)
         if line is not None:
             print(json.dumps(line), flush=True)
         if dist is not None:

@@ -70,7 +70,7 @@ def variant_count() -> int:
 def _units() -> list[tuple[str, str, list[str]]]:
     """(source, object name, extra flags) of every CUDA translation unit."""
     units = [(src, src.replace(".cu", ".o"), []) for src in CU_SOURCES]
-    for t in ("u32", "f32", "f64"):
+    for t in ("u32", "f32", "f64", "u64"):
         for v in range(variant_count()):
             units.append((VARIANT_TU, "gqs_v_%s_%d.o" % (t, v),
                           ["-DGQS_TU_LIST=GQS_VARIANTS_" + t.upper(), "-DGQS_TU_TYPE=" + t,

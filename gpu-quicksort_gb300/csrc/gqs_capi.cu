@@ -25,6 +25,7 @@ int variant_count(int dtype) {
     case DT_U32: return variant_count_u32();
     case DT_F32: return variant_count_f32();
     case DT_F64: return variant_count_f64();
+    case DT_U64: return variant_count_u64();
     default: return 0;
   }
 }
@@ -32,6 +33,7 @@ VariantInfo variant_info(int dtype, int v) {
   switch (dtype) {
     case DT_U32: return variant_info_u32(v);
     case DT_F32: return variant_info_f32(v);
+    case DT_U64: return variant_info_u64(v);
     default: return variant_info_f64(v);
   }
 }
@@ -39,6 +41,7 @@ int variant_prepare(int dtype, int v) {
   switch (dtype) {
     case DT_U32: return variant_prepare_u32(v);
     case DT_F32: return variant_prepare_f32(v);
+    case DT_U64: return variant_prepare_u64(v);
     default: return variant_prepare_f64(v);
   }
 }
@@ -46,6 +49,7 @@ cudaError_t launch_sort(int dtype, const LaunchParams& p) {
   switch (dtype) {
     case DT_U32: return launch_u32(p);
     case DT_F32: return launch_f32(p);
+    case DT_U64: return launch_u64(p);
     default: return launch_f64(p);
   }
 }
@@ -73,6 +77,10 @@ struct gqs_ctx {
   size_t pool_d_bytes = 0;
   void* pool_dn = nullptr;
   size_t pool_dn_bytes = 0;
+  void* pool_kv = nullptr;  // packed (key, value) words of the pair sort
+  size_t pool_kv_bytes = 0;
+  void* pool_v = nullptr;   // values staged for the host-pointer pair sort
+  size_t pool_v_bytes = 0;
   gqs::Job* jobs = nullptr;
   size_t job_cap = 0;
   gqs::Queue* q = nullptr;
@@ -90,8 +98,8 @@ struct gqs_ctx {
   unsigned long long pending_keys = 0;
   gqs_stats last{};
   uint64_t last_prof[32] = {};
-  int variant[3] = {0, 0, 0};
-  int blocks_per_sm[3][kMaxVariants] = {};
+  int variant[4] = {0, 0, 0, 0};  // per key type, and the internal packed pairs
+  int blocks_per_sm[4][kMaxVariants] = {};
 };
 
 namespace {
@@ -298,9 +306,119 @@ gqs_status sort_segments_host(gqs_ctx* c, int dtype, void* keys, size_t n, const
   return wait_pending_locked(c);
 }
 
+// ---- pair sort: (key, value) packed into one 64-bit word --------------------------------
+// word = (order-preserving key map << 32) | value, so sorting the words orders the pairs by key
+// and pairs with equal keys by value (values 0..n-1: a stable argsort).
+template <bool kFloat>
+__global__ void __launch_bounds__(256) pack_pairs(const uint32_t* __restrict__ keys,
+                                                  const uint32_t* __restrict__ vals,
+                                                  unsigned long long* __restrict__ out, size_t n) {
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    uint32_t k = keys[i];
+    if (kFloat) k ^= (uint32_t)((int32_t)k >> 31) | 0x80000000u;
+    out[i] = ((unsigned long long)k << 32) | vals[i];
+  }
+}
+
+template <bool kFloat>
+__global__ void __launch_bounds__(256) unpack_pairs(const unsigned long long* __restrict__ in,
+                                                    uint32_t* __restrict__ keys, uint32_t* __restrict__ vals,
+                                                    size_t n) {
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const unsigned long long w = in[i];
+    uint32_t k = (uint32_t)(w >> 32);
+    if (kFloat) k ^= ~(uint32_t)((int32_t)k >> 31) | 0x80000000u;
+    keys[i] = k;
+    vals[i] = (uint32_t)w;
+  }
+}
+
+// Enqueues pack -> sort of the words -> unpack on `stream` for device keys/values. Lock held.
+gqs_status enqueue_pairs_locked(gqs_ctx* c, bool is_float, uint32_t* keys, uint32_t* vals, size_t n,
+                                cudaStream_t stream) {
+  if ((reinterpret_cast<uintptr_t>(keys) & 3u) || (reinterpret_cast<uintptr_t>(vals) & 3u)) return GQS_ERR_INVALID;
+  if (n >= (1ull << 40)) return GQS_ERR_INVALID;
+  if (c->pool_kv_bytes < n * 8) {
+    (void)wait_pending_locked(c);
+    gqs_status st = grow(&c->pool_kv, &c->pool_kv_bytes, n * 8);
+    if (st != GQS_OK) return st;
+  }
+  const int blocks = c->num_sms * 8;
+  unsigned long long* w = static_cast<unsigned long long*>(c->pool_kv);
+  if (c->pending) {
+    cudaError_t e = cudaStreamWaitEvent(stream, c->ev_done, 0);  // the previous sort may still use pool_kv
+    if (e != cudaSuccess) return cuda_status(e);
+  }
+  if (is_float) pack_pairs<true><<<blocks, 256, 0, stream>>>(keys, vals, w, n);
+  else pack_pairs<false><<<blocks, 256, 0, stream>>>(keys, vals, w, n);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_status(e);
+  gqs_status st = enqueue_locked(c, gqs::DT_U64, w, nullptr, n, nullptr, 1, stream);
+  if (st != GQS_OK) return st;
+  if (is_float) unpack_pairs<true><<<blocks, 256, 0, stream>>>(w, keys, vals, n);
+  else unpack_pairs<false><<<blocks, 256, 0, stream>>>(w, keys, vals, n);
+  e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaEventRecord(c->ev_done, stream);  // the call is done after the unpack
+  return cuda_status(e);
+}
+
+gqs_status sort_pairs_dev(gqs_ctx* c, bool is_float, uint32_t* keys, uint32_t* vals, size_t n, void* stream) {
+  if (!c) return GQS_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(c->mu);
+  DeviceGuard dg(c->device);
+  if (n <= 1) return (keys && vals) || n == 0 ? GQS_OK : GQS_ERR_INVALID;
+  if (!keys || !vals) return GQS_ERR_INVALID;
+  gqs_status st = enqueue_pairs_locked(c, is_float, keys, vals, n, static_cast<cudaStream_t>(stream));
+  if (st != GQS_OK) return st;
+  if (c->cfg.sync) return wait_pending_locked(c);
+  return GQS_OK;
+}
+
+gqs_status sort_pairs_host(gqs_ctx* c, bool is_float, uint32_t* keys, uint32_t* vals, size_t n) {
+  if (!c) return GQS_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(c->mu);
+  DeviceGuard dg(c->device);
+  if (n <= 1) return (keys && vals) || n == 0 ? GQS_OK : GQS_ERR_INVALID;
+  if (!keys || !vals) return GQS_ERR_INVALID;
+  const size_t bytes = n * 4;
+  if (c->pool_d_bytes < bytes || c->pool_v_bytes < bytes) {
+    (void)wait_pending_locked(c);
+    gqs_status st = grow(&c->pool_d, &c->pool_d_bytes, bytes);
+    if (st == GQS_OK) st = grow(&c->pool_v, &c->pool_v_bytes, bytes);
+    if (st != GQS_OK) return st;
+  }
+  uint32_t* dk = static_cast<uint32_t*>(c->pool_d);
+  uint32_t* dv = static_cast<uint32_t*>(c->pool_v);
+  cudaError_t e = cudaMemcpyAsync(dk, keys, bytes, cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dv, vals, bytes, cudaMemcpyHostToDevice, c->stream);
+  if (e != cudaSuccess) return cuda_status(e);
+  gqs_status st = enqueue_pairs_locked(c, is_float, dk, dv, n, c->stream);
+  if (st != GQS_OK) return st;
+  e = cudaMemcpyAsync(keys, dk, bytes, cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(vals, dv, bytes, cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaEventRecord(c->ev_done, c->stream);
+  if (e != cudaSuccess) return cuda_status(e);
+  return wait_pending_locked(c);
+}
+
 }  // namespace
 
 extern "C" {
+
+gqs_status gqs_sort_pairs_u32(gqs_ctx* c, uint32_t* keys, uint32_t* values, size_t n) {
+  return sort_pairs_host(c, false, keys, values, n);
+}
+gqs_status gqs_sort_pairs_f32(gqs_ctx* c, float* keys, uint32_t* values, size_t n) {
+  return sort_pairs_host(c, true, reinterpret_cast<uint32_t*>(keys), values, n);
+}
+gqs_status gqs_sort_pairs_u32_dev(gqs_ctx* c, uint32_t* keys, uint32_t* values, size_t n, void* stream) {
+  return sort_pairs_dev(c, false, keys, values, n, stream);
+}
+gqs_status gqs_sort_pairs_f32_dev(gqs_ctx* c, float* keys, uint32_t* values, size_t n, void* stream) {
+  return sort_pairs_dev(c, true, reinterpret_cast<uint32_t*>(keys), values, n, stream);
+}
 
 void gqs_config_default(gqs_config* cfg) {
   if (!cfg) return;
@@ -334,7 +452,7 @@ gqs_status gqs_create(gqs_ctx** out, int device, const gqs_config* cfg) {
     }
     if (cudaMalloc(&c->q, sizeof(gqs::Queue)) != cudaSuccess) { st = GQS_ERR_NOMEM; break; }
     if (cudaMallocHost(&c->q_host, sizeof(gqs::Queue)) != cudaSuccess) { st = GQS_ERR_NOMEM; break; }
-    for (int t = 0; t < 3; ++t) {
+    for (int t = 0; t < 4; ++t) {
       int v = c->cfg.variant;
       if (v < 0 || v >= gqs::variant_count(t)) v = 0;
       c->variant[t] = v;
@@ -356,6 +474,8 @@ void gqs_destroy(gqs_ctx* c) {
     if (c->pending && c->ev_done) cudaEventSynchronize(c->ev_done);
     if (c->pool_d) cudaFree(c->pool_d);
     if (c->pool_dn) cudaFree(c->pool_dn);
+    if (c->pool_kv) cudaFree(c->pool_kv);
+    if (c->pool_v) cudaFree(c->pool_v);
     if (c->jobs) cudaFree(c->jobs);
     if (c->q) cudaFree(c->q);
     if (c->offs) cudaFree(c->offs);

@@ -128,6 +128,14 @@ struct KeyOps<float> {
   static __device__ __forceinline__ B raw(B k) { return k ^ (~(uint32_t)((int32_t)k >> 31) | 0x80000000u); }
   static constexpr bool kIdentity = false;
 };
+// 64-bit unsigned keys: the packed (key, value) words of the pair sort.
+template <>
+struct KeyOps<uint64_t> {
+  using B = uint64_t;
+  static __device__ __forceinline__ B key(B v) { return v; }
+  static __device__ __forceinline__ B raw(B k) { return k; }
+  static constexpr bool kIdentity = true;
+};
 template <>
 struct KeyOps<double> {
   using B = uint64_t;

@@ -12,7 +12,7 @@
 
 namespace gqs {
 
-constexpr size_t kElemSize[3] = {4, 4, 8};
+constexpr size_t kElemSize[4] = {4, 4, 8, 8};  // u32, f32, f64, and the internal u64
 
 inline gqs_status cuda_status(cudaError_t e) {
   if (e == cudaSuccess) return GQS_OK;

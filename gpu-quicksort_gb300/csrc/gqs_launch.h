@@ -10,7 +10,8 @@ namespace gqs {
 struct Job;
 struct Queue;
 
-enum DType : int { DT_U32 = 0, DT_F32 = 1, DT_F64 = 2 };
+// DT_U64 is internal: the packed words of the pair sort (gqs_sort_pairs_*).
+enum DType : int { DT_U32 = 0, DT_F32 = 1, DT_F64 = 2, DT_U64 = 3 };
 
 struct VariantInfo {
   int ncw;         // consumer warps per CTA
@@ -54,6 +55,7 @@ struct LaunchParams {
 GQS_DECLARE_TYPE(u32)
 GQS_DECLARE_TYPE(f32)
 GQS_DECLARE_TYPE(f64)
+GQS_DECLARE_TYPE(u64)
 #undef GQS_DECLARE_TYPE
 
 // Dispatch by key type (defined in gqs_capi.cu).

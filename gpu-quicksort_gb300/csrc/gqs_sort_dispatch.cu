@@ -11,6 +11,7 @@ namespace gqs {
 GQS_VARIANTS_U32(GQS_DECL)
 GQS_VARIANTS_F32(GQS_DECL)
 GQS_VARIANTS_F64(GQS_DECL)
+GQS_VARIANTS_U64(GQS_DECL)
 #undef GQS_DECL
 
 #define GQS_CASE_INFO(S, V, ...) \
@@ -50,5 +51,6 @@ GQS_VARIANTS_F64(GQS_DECL)
 GQS_TYPE_TABLE(u32, GQS_VARIANTS_U32)
 GQS_TYPE_TABLE(f32, GQS_VARIANTS_F32)
 GQS_TYPE_TABLE(f64, GQS_VARIANTS_F64)
+GQS_TYPE_TABLE(u64, GQS_VARIANTS_U64)
 
 }  // namespace gqs

@@ -24,4 +24,12 @@
   X(f64, 3, double, 16, 8192, 2048, 3, 4, 2048)              \
   X(f64, 4, double, 8, 6144, 2048, 3, 4, 2048)               \
   X(f64, 5, double, 8, 2048, 1024, 4, 4, 2048)
+// Packed (key, value) words of the pair sort: the f64 geometry with an identity key map.
+#define GQS_VARIANTS_U64(X)                                  \
+  X(u64, 0, uint64_t, 16, 6144, 4096, 3, 4, 2048)            \
+  X(u64, 1, uint64_t, 24, 6144, 3072, 3, 4, 2048)            \
+  X(u64, 2, uint64_t, 16, 4096, 4096, 4, 4, 2048)            \
+  X(u64, 3, uint64_t, 16, 8192, 2048, 3, 4, 2048)            \
+  X(u64, 4, uint64_t, 8, 6144, 2048, 3, 4, 2048)             \
+  X(u64, 5, uint64_t, 8, 2048, 1024, 4, 4, 2048)
 #define GQS_VARIANT_COUNT 6

@@ -37,6 +37,7 @@ EXPORTS = [
     "gqs_srv_config_default", "gqs_srv_create", "gqs_srv_destroy", "gqs_srv_submit", "gqs_srv_wait",
     "gqs_srv_wait_any", "gqs_srv_cancel", "gqs_srv_drain", "gqs_srv_stats", "gqs_srv_now_ns",
     "gqs_selftest_stalled_queue",
+    "gqs_sort_pairs_u32", "gqs_sort_pairs_f32", "gqs_sort_pairs_u32_dev", "gqs_sort_pairs_f32_dev",
 ]
 
 
@@ -127,6 +128,13 @@ def load_library(path: str | None = None) -> C.CDLL:
         f.restype = st
         f = getattr(lib, f"gqs_sort_segments_{t}")
         f.argtypes = [vp, vp, sz, vp, sz]
+        f.restype = st
+    for t in ("u32", "f32"):
+        f = getattr(lib, f"gqs_sort_pairs_{t}")
+        f.argtypes = [vp, vp, vp, sz]
+        f.restype = st
+        f = getattr(lib, f"gqs_sort_pairs_{t}_dev")
+        f.argtypes = [vp, vp, vp, sz, vp]
         f.restype = st
     lib.gqs_sort_u32_noalloc.argtypes = [vp, sz, vp]
     lib.gqs_sort_u32_noalloc.restype = st
@@ -245,6 +253,25 @@ class Context:
         t = _np_tag(a)
         assert a.flags.c_contiguous
         _check(getattr(self.lib, f"gqs_sort_{t}")(self.h, _ptr(a), None, a.size), f"gqs_sort_{t}")
+
+    def sort_pairs(self, keys: np.ndarray, values: np.ndarray) -> None:
+        """Sorts (key, value) pairs in place by key (uint32 or float32 keys, uint32 values)."""
+        t = _np_tag(keys)
+        if t not in ("u32", "f32") or values.dtype != np.uint32 or values.size != keys.size:
+            raise TypeError("pairs are uint32/float32 keys with uint32 values of the same length")
+        assert keys.flags.c_contiguous and values.flags.c_contiguous
+        _check(getattr(self.lib, f"gqs_sort_pairs_{t}")(self.h, _ptr(keys), _ptr(values), keys.size),
+               f"gqs_sort_pairs_{t}")
+
+    def argsort(self, keys: np.ndarray) -> np.ndarray:
+        """Stable argsort of uint32/float32 keys (keys are left untouched)."""
+        k = keys.copy()
+        idx = np.arange(keys.size, dtype=np.uint32)
+        self.sort_pairs(k, idx)
+        return idx
+
+    def sort_pairs_dev(self, dtype: str, keys: int, values: int, n: int, stream: int = 0) -> int:
+        return getattr(self.lib, f"gqs_sort_pairs_{dtype}_dev")(self.h, keys, values, n, stream or None)
 
     def sort_segments(self, a: np.ndarray, offsets: np.ndarray) -> None:
         t = _np_tag(a)

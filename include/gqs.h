@@ -119,6 +119,18 @@ gqs_status gqs_sort_segments_u32(gqs_ctx* ctx, uint32_t* keys, size_t n, const u
 gqs_status gqs_sort_segments_f32(gqs_ctx* ctx, float* keys, size_t n, const uint64_t* offsets, size_t nseg);
 gqs_status gqs_sort_segments_f64(gqs_ctx* ctx, double* keys, size_t n, const uint64_t* offsets, size_t nseg);
 
+/* Key-value sorts: n (key, value) pairs, keys uint32 or float, values uint32, sorted by key with
+ * every value travelling with its key. Pairs with equal keys come out in ascending value order,
+ * so values 0..n-1 give a stable argsort (the sorting permutation). Host-pointer forms sort both
+ * host arrays in place; *_dev forms take device arrays and a stream (cfg.sync as above). Each
+ * pair is packed into one 64-bit word (the key's order-preserving map above the value) and
+ * the words are sorted by the same persistent kernel. No reference counterpart: the reference
+ * sorts keys only; this is the key-value variant of its GPUQSort<T> path. */
+gqs_status gqs_sort_pairs_u32(gqs_ctx* ctx, uint32_t* keys, uint32_t* values, size_t n);
+gqs_status gqs_sort_pairs_f32(gqs_ctx* ctx, float* keys, uint32_t* values, size_t n);
+gqs_status gqs_sort_pairs_u32_dev(gqs_ctx* ctx, uint32_t* keys, uint32_t* values, size_t n, void* stream);
+gqs_status gqs_sort_pairs_f32_dev(gqs_ctx* ctx, float* keys, uint32_t* values, size_t n, void* stream);
+
 /* Largest n accepted by gqs_sort_u32_noalloc. */
 #define GQS_NOALLOC_MAX_KEYS (1u << 20)
 
