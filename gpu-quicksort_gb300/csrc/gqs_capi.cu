@@ -59,6 +59,10 @@ cudaError_t launch_sort(int dtype, const LaunchParams& p) {
 namespace {
 
 constexpr int kMaxVariants = 16;
+// Host-pointer sorts of at least kPipeMin keys are pipelined: the array is copied in kPieces
+// pieces, each sorted as soon as it has arrived, then the sorted pieces are merged.
+constexpr size_t kPipeMin = 1ull << 24;
+constexpr int kPieces = 4;
 using gqs::cuda_status;
 using gqs::DeviceGuard;
 using gqs::job_capacity;
@@ -72,7 +76,13 @@ struct gqs_ctx {
   int num_sms = 0;
   gqs_config cfg{};
   std::mutex mu;
-  cudaStream_t stream = nullptr;  // used by the host-pointer calls
+  cudaStream_t stream = nullptr;       // used by the host-pointer calls
+  cudaStream_t copy_stream = nullptr;  // host -> device pieces of a pipelined host sort
+  cudaEvent_t ev_piece[4] = {};
+  gqs::Queue* q_acc = nullptr;         // statistics of a pipelined sort, summed over its pieces
+  void* merge_splits = nullptr;        // merge-path splits of the pipelined sort's merges
+  size_t merge_splits_bytes = 0;
+  bool pending_acc = false;
   void* pool_d = nullptr;
   size_t pool_d_bytes = 0;
   void* pool_dn = nullptr;
@@ -125,8 +135,9 @@ gqs_status wait_pending_locked(gqs_ctx* c) {
   if (!c->pending) return GQS_OK;
   cudaError_t e = cudaEventSynchronize(c->ev_done);
   if (e != cudaSuccess) return cuda_status(e);
-  e = cudaMemcpy(c->q_host, c->q, sizeof(gqs::Queue), cudaMemcpyDeviceToHost);
+  e = cudaMemcpy(c->q_host, c->pending_acc ? c->q_acc : c->q, sizeof(gqs::Queue), cudaMemcpyDeviceToHost);
   c->pending = false;
+  c->pending_acc = false;
   if (e != cudaSuccess) return cuda_status(e);
   gqs_stats s = gqs::stats_from_queue(*c->q_host, c->pending_dtype, c->pending_variant, c->pending_grid);
   if (c->pending_timed) {
@@ -234,12 +245,82 @@ gqs_status sort_dev(gqs_ctx* c, int dtype, void* d, void* scratch, size_t n, voi
   return GQS_OK;
 }
 
+// Folds one piece's status block into the pipelined sort's totals (one thread).
+__global__ void accumulate_queue(const gqs::Queue* __restrict__ q, gqs::Queue* __restrict__ acc) {
+  acc->total += q->total;
+  acc->done += q->done;
+  acc->part_keys += q->part_keys;
+  acc->local_keys += q->local_keys;
+  acc->tiny_keys += q->tiny_keys;
+  acc->fill_keys += q->fill_keys;
+  acc->chunks += q->chunks;
+  acc->part_jobs += q->part_jobs;
+  acc->local_jobs += q->local_jobs;
+  acc->fill_jobs += q->fill_jobs;
+  if (q->max_depth > acc->max_depth) acc->max_depth = q->max_depth;
+  if (q->error && !acc->error) {
+    acc->error = q->error;
+    acc->error_info = q->error_info;
+  }
+}
+
+// The host-pointer sort of a large array, overlapping the copy in with the sort: piece i is
+// copied on the copy stream while piece i - 1 is sorted; the sorted pieces are merged pairwise
+// (two merge passes for four pieces) and the result copied back. Lock held.
+gqs_status sort_host_pipelined(gqs_ctx* c, int dtype, void* d, size_t n) {
+  const size_t es = kElemSize[dtype];
+  const size_t bytes = n * es;
+  const size_t split_bytes = gqs::merge_split_words(n) * sizeof(unsigned long long);
+  if (c->pool_d_bytes < bytes || c->pool_dn_bytes < bytes || c->merge_splits_bytes < split_bytes) {
+    (void)wait_pending_locked(c);
+    gqs_status st = grow(&c->pool_d, &c->pool_d_bytes, bytes);
+    if (st == GQS_OK) st = grow(&c->pool_dn, &c->pool_dn_bytes, bytes);
+    if (st == GQS_OK) st = grow(&c->merge_splits, &c->merge_splits_bytes, split_bytes);
+    if (st != GQS_OK) return st;
+  }
+  unsigned long long* sp = static_cast<unsigned long long*>(c->merge_splits);
+  size_t off[kPieces + 1];
+  for (int i = 0; i <= kPieces; ++i) off[i] = n / kPieces * i;
+  off[kPieces] = n;
+  char* dd = static_cast<char*>(c->pool_d);
+  char* dn = static_cast<char*>(c->pool_dn);
+  char* hd = static_cast<char*>(d);
+  cudaError_t e = cudaSuccess;
+  if (c->pending) e = cudaStreamWaitEvent(c->copy_stream, c->ev_done, 0);  // pool_d is free again
+  if (e == cudaSuccess) e = cudaMemsetAsync(c->q_acc, 0, sizeof(gqs::Queue), c->stream);
+  if (e != cudaSuccess) return cuda_status(e);
+  for (int i = 0; i < kPieces; ++i) {
+    const size_t len = off[i + 1] - off[i];
+    e = cudaMemcpyAsync(dd + off[i] * es, hd + off[i] * es, len * es, cudaMemcpyHostToDevice, c->copy_stream);
+    if (e == cudaSuccess) e = cudaEventRecord(c->ev_piece[i], c->copy_stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(c->stream, c->ev_piece[i], 0);
+    if (e != cudaSuccess) return cuda_status(e);
+    gqs_status st = enqueue_locked(c, dtype, dd + off[i] * es, dn + off[i] * es, len, nullptr, 1, c->stream);
+    if (st != GQS_OK) return st;
+    accumulate_queue<<<1, 1, 0, c->stream>>>(c->q, c->q_acc);
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_status(e);
+  }
+  // pieces 0+1 and 2+3 into the scratch, then the two halves back into pool_d
+  e = gqs::merge_runs(dtype, dd, off[1], dd + off[1] * es, off[2] - off[1], dn, sp, c->stream);
+  if (e == cudaSuccess)
+    e = gqs::merge_runs(dtype, dd + off[2] * es, off[3] - off[2], dd + off[3] * es, off[4] - off[3], dn + off[2] * es,
+                        sp, c->stream);
+  if (e == cudaSuccess) e = gqs::merge_runs(dtype, dn, off[2], dn + off[2] * es, n - off[2], dd, sp, c->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d, dd, bytes, cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaEventRecord(c->ev_done, c->stream);
+  if (e != cudaSuccess) return cuda_status(e);
+  c->pending_acc = true;
+  c->pending_timed = false;
+  return wait_pending_locked(c);
+}
+
 gqs_status sort_host(gqs_ctx* c, int dtype, void* d, size_t n) {
   if (!c) return GQS_ERR_INVALID;
   std::lock_guard<std::mutex> lk(c->mu);
   DeviceGuard dg(c->device);
   if (n <= 1) return d || n == 0 ? GQS_OK : GQS_ERR_INVALID;
   if (!d) return GQS_ERR_INVALID;
+  if (n >= kPipeMin && n < (1ull << 40)) return sort_host_pipelined(c, dtype, d, n);
   const size_t bytes = n * kElemSize[dtype];
   if (c->pool_d_bytes < bytes) {
     gqs_status st = wait_pending_locked(c);
@@ -444,7 +525,15 @@ gqs_status gqs_create(gqs_ctx** out, int device, const gqs_config* cfg) {
   DeviceGuard dg(device);
   gqs_status st = GQS_OK;
   do {
-    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) { st = GQS_ERR_CUDA; break; }
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking) != cudaSuccess) {
+      st = GQS_ERR_CUDA;
+      break;
+    }
+    bool evs = true;
+    for (cudaEvent_t& ev : c->ev_piece) evs = evs && cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) == cudaSuccess;
+    if (!evs) { st = GQS_ERR_CUDA; break; }
+    if (cudaMalloc(&c->q_acc, sizeof(gqs::Queue)) != cudaSuccess) { st = GQS_ERR_NOMEM; break; }
     if (cudaEventCreate(&c->ev_begin) != cudaSuccess || cudaEventCreate(&c->ev_end) != cudaSuccess ||
         cudaEventCreateWithFlags(&c->ev_done, cudaEventDisableTiming) != cudaSuccess) {
       st = GQS_ERR_CUDA;
@@ -485,6 +574,11 @@ void gqs_destroy(gqs_ctx* c) {
     if (c->ev_end) cudaEventDestroy(c->ev_end);
     if (c->ev_done) cudaEventDestroy(c->ev_done);
     if (c->stream) cudaStreamDestroy(c->stream);
+    if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
+    for (cudaEvent_t ev : c->ev_piece)
+      if (ev) cudaEventDestroy(ev);
+    if (c->q_acc) cudaFree(c->q_acc);
+    if (c->merge_splits) cudaFree(c->merge_splits);
   }
   delete c;
 }

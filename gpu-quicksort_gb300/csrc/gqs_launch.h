@@ -64,5 +64,10 @@ VariantInfo variant_info(int dtype, int v);
 // Sets the shared-memory attribute and returns the resident CTAs per SM (0 if it cannot run).
 int variant_prepare(int dtype, int v);
 cudaError_t launch_sort(int dtype, const LaunchParams& p);
+// Merges sorted runs a[0, na) and b[0, nb) of key type dtype into out (defined in gqs_merge.cu);
+// `splits` is device scratch of merge_split_words(na + nb) words.
+size_t merge_split_words(size_t total);
+cudaError_t merge_runs(int dtype, const void* a, size_t na, const void* b, size_t nb, void* out,
+                       unsigned long long* splits, cudaStream_t s);
 
 }  // namespace gqs

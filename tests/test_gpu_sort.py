@@ -226,3 +226,17 @@ def test_all_variants(dtype):
                     assert ctx.stats()["variant"] == v["index"]
         finally:
             ctx.close()
+
+
+@pytest.mark.parametrize("dtype,dist,n", [("u32", "uniform", 1 << 24), ("u32", "distinct16", (1 << 24) + 5),
+                                          ("u32", "sorted", 3 * (1 << 23) + 7), ("f32", "gaussian", (1 << 24) + 3),
+                                          ("f64", "uniform", (1 << 24) + 1), ("u32", "reverse", 1 << 25)])
+def test_pipelined_host_sort(gpu_ctx, dtype, dist, n):
+    """Host-pointer sorts of 2^24 keys and more are copied in four pieces, each sorted as soon as
+    it arrives, and the sorted pieces merged: the result is the same as a single sort."""
+    x = gqs_ctypes.generate(dtype, dist, 123 + n, n)
+    y = x.copy()
+    gpu_ctx.sort(y)
+    assert np.array_equal(y.view(np.uint8), np.sort(x).view(np.uint8))
+    st = gpu_ctx.stats()
+    assert st["status"] == 0 and st["keys"] == n
