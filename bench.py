@@ -178,12 +178,20 @@ def cpu_baseline(args, n_full):
     t2 = time.perf_counter()
     oracle_ctypes.cpu_quicksort(d)
     t_q = time.perf_counter() - t2
+    # the reference's parallel CPU sort (tbb::parallel_sort, QuicksortMain.cpp:993), here GCC's
+    # parallel mode sort on all threads
+    e = a.copy()
+    t3 = time.perf_counter()
+    oracle_ctypes.parallel_sort(e, threads)
+    t_p = time.perf_counter() - t3
     return {"value": ns / t / 1e9, "unit": "Gkeys/s", "cores": threads, "kind": "port",
             "sample": f"GPUQSort<T> restatement (oracle/gqs_oracle.cpp) on {ns} {args.dtype} keys of the same "
                       f"distribution, {threads} threads, one sort of {t:.3f} s",
             "std_sort_1core": {"value": ns1 / t_std / 1e9, "unit": "Gkeys/s", "keys": ns1},
             "reference_cpu_quicksort_1core": {"value": ns1 / t_q / 1e9, "unit": "Gkeys/s", "keys": ns1,
                                               "bit_exact_vs_std_sort": bool(np.array_equal(c, d))},
+            "parallel_sort_all_cores": {"value": ns / t_p / 1e9, "unit": "Gkeys/s", "keys": ns, "threads": threads,
+                                        "what": "__gnu_parallel::sort, standing in for tbb::parallel_sort"},
             "cpu": platform.processor() or platform.machine()}
 
 
