@@ -162,7 +162,7 @@ struct SortArgs {
 
 // Kernel configuration. TILE keys fit one local (on-chip) sort; CHUNK keys are one staged
 // partition chunk; TINY = 32*R keys are sorted in registers by one warp.
-template <class T_, int NCW_, int TILE_, int CHUNK_, int STAGES_, int R_, int WARP_MAX_>
+template <class T_, int NCW_, int TILE_, int CHUNK_, int STAGES_, int R_>
 struct Cfg {
   using T = T_;
   using Ops = KeyOps<T>;
@@ -175,7 +175,6 @@ struct Cfg {
   static constexpr int STAGES = STAGES_;
   static constexpr int R = R_;
   static constexpr int TINY = 32 * R;
-  static constexpr int WARP_MAX = WARP_MAX_;
   static constexpr int KPT = CHUNK / NC;
   static constexpr int E16 = 16 / (int)sizeof(B);
   static constexpr int STAGE_ELEMS = CHUNK + 2 * E16;
@@ -199,10 +198,6 @@ struct Cfg {
   static_assert(TILE > TINY, "tile must exceed the register sort");
   static_assert(NB_MAX <= 256 && NB_MAX >= 32, "bucket labels are bytes; the scan takes 32..256 buckets");
   static_assert(SPLIT_SAMPLES % 32 == 0 && SPLIT_SAMPLES >= NB_MAX, "samples per lane; one pivot per bucket");
-};
-
-struct Seg {
-  uint32_t s, e, buf;
 };
 
 // A segment of the on-chip tile being partitioned slice by slice (shared memory).
@@ -565,7 +560,6 @@ struct Persistent {
   using Ops = typename C::Ops;
 
   static __device__ __forceinline__ void cbar() { named_bar_sync(1, C::NC); }
-  static __device__ __forceinline__ bool tid0_of_cta() { return threadIdx.x == 0; }
 
   // ---- producer ---------------------------------------------------------
   // Work is taken by ticket: one atomic on the queue's grab counter reserves kTake consecutive

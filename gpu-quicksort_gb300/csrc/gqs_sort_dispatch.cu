@@ -4,7 +4,7 @@
 
 namespace gqs {
 
-#define GQS_DECL(S, V, T, NCW, TILE, CHUNK, STAGES, R, WM) \
+#define GQS_DECL(S, V, T, NCW, TILE, CHUNK, STAGES, R) \
   VariantInfo info_##S##_##V();                            \
   int prepare_##S##_##V();                                 \
   cudaError_t launch_##S##_##V(const LaunchParams& p);

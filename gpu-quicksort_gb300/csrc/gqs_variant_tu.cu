@@ -16,10 +16,10 @@ namespace gqs {
 namespace {
 template <int I>
 struct Pick;
-#define GQS_PICK(S, V, T, NCW, TILE, CHUNK, STAGES, R, WM)                            \
+#define GQS_PICK(S, V, T, NCW, TILE, CHUNK, STAGES, R)                                \
   template <>                                                                         \
   struct Pick<V> {                                                                    \
-    using C = Cfg<T, NCW, TILE, CHUNK, STAGES, R, WM>;                                \
+    using C = Cfg<T, NCW, TILE, CHUNK, STAGES, R>;                                    \
     static const char* name() { return #S "_ncw" #NCW "_tile" #TILE "_chunk" #CHUNK "_st" #STAGES; } \
   };
 GQS_TU_LIST(GQS_PICK)
