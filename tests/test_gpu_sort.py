@@ -69,7 +69,9 @@ def test_golden_vectors(gpu_ctx, case):
 
 @pytest.mark.parametrize("dtype", ["u32", "f32", "f64"])
 def test_known_answer(gpu_ctx, dtype):
-    for n in (1, 2, 1024, 1 << 16, 1 << 20, 3_000_000):
+    # sizes up to the reference's own CTest run of its shuffled 1..N check, N = 2^22
+    # (GPU-Quicksort_OpenCL_1.2/CMakeLists.txt:42-44, check at QuicksortMain.cpp:415-416)
+    for n in (1, 2, 1024, 1 << 16, 1 << 20, 3_000_000, 1 << 22):
         a = gqs_ctypes.generate(dtype, "kat", 5, n)
         gpu_ctx.sort(a)
         assert np.array_equal(a, np.arange(1, n + 1, dtype=a.dtype))
@@ -207,6 +209,16 @@ def test_full_size_configs(gpu_ctx, dtype, dist, n):
     assert st["status"] == 0 and st["keys"] == n
     del t, ref, got
     torch.cuda.empty_cache()
+
+
+# The largest arrays: the top of the reference's benchmark sweep, 2 x 16384 x 16384 = 2^29
+# keys (build_me.sh:3-20), and 2 GiB of doubles and 2 GiB of floats.
+MAXSIZE = [("u32", "uniform", 1 << 29), ("f64", "uniform", 1 << 28), ("f32", "gaussian", 1 << 29)]
+
+
+@pytest.mark.parametrize("dtype,dist,n", MAXSIZE, ids=lambda x: str(x))
+def test_maximum_sizes(gpu_ctx, dtype, dist, n):
+    test_full_size_configs(gpu_ctx, dtype, dist, n)
 
 
 # ---------------------------------------------------------------------------
