@@ -381,62 +381,89 @@ __device__ __forceinline__ K kmax() {
 // ---------------------------------------------------------------------------
 // Queue operations.
 
-// Publishes one job; called by all 32 lanes of a warp with the same arguments. Lane 0 writes
-// the record, then every lane writes a share of its ticket-map entries.
+// Publishes `njobs` (1 or 2) jobs with one allocation: consecutive record slots, and each
+// job's tickets after the previous job's. Called by all 32 lanes of a warp with the same
+// arguments. Lane 0 writes the records, then every lane writes a share of the ticket-map
+// entries. The two children of a finished partition go out together, so the completer pays
+// one allocation round trip and one fence for both.
 template <class C>
-__device__ bool push_job(const SortArgs<typename C::T>& a, uint32_t kind, uint32_t dir,
-                         unsigned long long start, unsigned long long end, unsigned long long pivot,
-                         uint32_t depth) {
+__device__ bool push_jobs(const SortArgs<typename C::T>& a, uint32_t njobs, const uint32_t (&kind)[2], uint32_t dir,
+                          const unsigned long long (&start)[2], const unsigned long long (&end)[2],
+                          const unsigned long long (&pivot)[2], uint32_t depth) {
   using B = typename C::B;
   const int lane = threadIdx.x & 31;
-  long long grid = (long long)start;
-  uint32_t nch = 1;
-  if (kind == JOB_PART) {
-    const B* src = dir ? a.d : a.dn;
-    grid -= (long long)((reinterpret_cast<uintptr_t>(src + start) & 15u) / sizeof(B));
-    nch = (uint32_t)(((long long)end - grid + C::CHUNK - 1) / C::CHUNK);
-  } else if (kind == JOB_FILL) {
-    grid -= (long long)((reinterpret_cast<uintptr_t>(a.d + start) & 15u) / sizeof(B));
-    nch = (uint32_t)(((long long)end - grid + C::FILL_CHUNK - 1) / C::FILL_CHUNK);
+  long long grid[2];
+  uint32_t nch[2];
+#pragma unroll
+  for (int i = 0; i < 2; ++i) {
+    grid[i] = (long long)start[i];
+    nch[i] = 0;
+    if ((uint32_t)i >= njobs) continue;
+    nch[i] = 1;
+    if (kind[i] == JOB_PART) {
+      const B* src = dir ? a.d : a.dn;
+      grid[i] -= (long long)((reinterpret_cast<uintptr_t>(src + start[i]) & 15u) / sizeof(B));
+      nch[i] = (uint32_t)(((long long)end[i] - grid[i] + C::CHUNK - 1) / C::CHUNK);
+    } else if (kind[i] == JOB_FILL) {
+      grid[i] -= (long long)((reinterpret_cast<uintptr_t>(a.d + start[i]) & 15u) / sizeof(B));
+      nch[i] = (uint32_t)(((long long)end[i] - grid[i] + C::FILL_CHUNK - 1) / C::FILL_CHUNK);
+    }
   }
+  const uint32_t total = nch[0] + nch[1];
   unsigned long long old = 0;
   uint32_t ok = 1;
   if (lane == 0) {
-    old = atomicAdd(&a.q->alloc, (1ull << 32) | (unsigned long long)nch);
+    // `grab` is read before the allocation: an older value only overstates the untaken tickets
+    const uint32_t grab = ld_relaxed(&a.q->grab);
+    old = atomicAdd(&a.q->alloc, ((unsigned long long)njobs << 32) | (unsigned long long)total);
     const uint32_t slot = (uint32_t)(old >> 32), t0 = (uint32_t)old;
     // the ring must still hold every ticket not yet taken once these are added (producers
-    // may hold tickets ahead of the last one created, so `grab` can exceed t0 + nch)
-    const long long untaken = (long long)t0 + (long long)nch - (long long)ld_relaxed(&a.q->grab);
-    if (slot >= a.capacity || untaken > (long long)a.tmask + 1) {
+    // may hold tickets ahead of the last one created, so `grab` can exceed t0 + total)
+    const long long untaken = (long long)t0 + (long long)total - (long long)grab;
+    if ((unsigned long long)slot + njobs > a.capacity || untaken > (long long)a.tmask + 1) {
       set_error(a.q, ST_CAPACITY, slot);
       ok = 0;
     } else {
-      Job* j = a.jobs + slot;
-      j->start = start;
-      j->end = end;
-      j->sstart = start;
-      j->send = end;
-      j->pivot = pivot;
-      j->grid = grid;
-      j->kind = kind;
-      j->dir = dir;
-      j->nchunks = nch;
-      j->t0 = t0;
-      j->remaining = nch;
-      j->depth = depth;
+#pragma unroll
+      for (int i = 0; i < 2; ++i) {
+        if ((uint32_t)i >= njobs) continue;
+        Job* j = a.jobs + slot + i;
+        j->start = start[i];
+        j->end = end[i];
+        j->sstart = start[i];
+        j->send = end[i];
+        j->pivot = pivot[i];
+        j->grid = grid[i];
+        j->kind = kind[i];
+        j->dir = dir;
+        j->nchunks = nch[i];
+        j->t0 = t0 + (i ? nch[0] : 0u);
+        j->remaining = nch[i];
+        j->depth = depth;
+      }
     }
   }
   ok = __shfl_sync(0xffffffffu, ok, 0);
   old = __shfl_sync(0xffffffffu, old, 0);
   if (!ok) return false;
   __syncwarp();
-  __threadfence();  // the record (written by lane 0, ordered by the warp barrier) before its tickets
+  __threadfence();  // the records (written by lane 0, ordered by the warp barrier) before their tickets
   const uint32_t slot = (uint32_t)(old >> 32), t0 = (uint32_t)old;
-  for (uint32_t i = lane; i < nch; i += 32) {
+  for (uint32_t i = lane; i < total; i += 32) {
     const uint32_t t = t0 + i;
-    st_relaxed(a.tmap + (t & a.tmask), ((unsigned long long)(t + 1) << 32) | slot);
+    st_relaxed(a.tmap + (t & a.tmask), ((unsigned long long)(t + 1) << 32) | (slot + (i < nch[0] ? 0u : 1u)));
   }
   return true;
+}
+
+// Publishes one job (see push_jobs).
+template <class C>
+__device__ bool push_job(const SortArgs<typename C::T>& a, uint32_t kind, uint32_t dir,
+                         unsigned long long start, unsigned long long end, unsigned long long pivot,
+                         uint32_t depth) {
+  const uint32_t k[2] = {kind, 0u};
+  const unsigned long long s[2] = {start, 0ull}, e[2] = {end, 0ull}, p[2] = {pivot, 0ull};
+  return push_jobs<C>(a, 1u, k, dir, s, e, p, depth);
 }
 
 // Median of 32*RS evenly spaced samples of src[a, a+m) (global memory, L2 reads).
@@ -453,6 +480,31 @@ __device__ typename C::B sample_pivot_global(const typename C::B* src, unsigned 
   }
   warp_bitonic<RS>(v);
   return __shfl_sync(0xffffffffu, v[0], 16);
+}
+
+// The pivots of two ranges at once (each as sample_pivot_global computes it): every lane
+// issues its loads for both ranges before either network runs. `use0`/`use1` are warp-uniform.
+template <class C, int RS>
+__device__ void sample_pivots_global2(const typename C::B* src, unsigned long long a0, unsigned long long m0,
+                                      bool use0, unsigned long long a1, unsigned long long m1, bool use1,
+                                      typename C::B& p0, typename C::B& p1) {
+  using B = typename C::B;
+  const int lane = threadIdx.x & 31;
+  B v0[RS], v1[RS];
+#pragma unroll
+  for (int r = 0; r < RS; ++r) {
+    const unsigned long long idx = (unsigned long long)(lane * RS + r);
+    v0[r] = use0 ? C::Ops::key(__ldcg(src + a0 + (idx * m0) / (32ull * RS))) : B(0);
+    v1[r] = use1 ? C::Ops::key(__ldcg(src + a1 + (idx * m1) / (32ull * RS))) : B(0);
+  }
+  if (use0) {
+    warp_bitonic<RS>(v0);
+    p0 = __shfl_sync(0xffffffffu, v0[0], 16);
+  }
+  if (use1) {
+    warp_bitonic<RS>(v1);
+    p1 = __shfl_sync(0xffffffffu, v1[0], 16);
+  }
 }
 
 // One warp sorts src[a, a+m) (m <= 32*R) into d[a, a+m) with a network of 32*R keys.
@@ -484,31 +536,46 @@ __device__ __forceinline__ void warp_sort_global(const typename C::B* src, typen
   else warp_sort_global_r<C, C::R>(src, d, a, m);
 }
 
-// Decide what to do with a range whose keys sit in `src` (dir says which buffer that is).
+// What becomes of a range of m keys: 0 = placed at once by place_small (at most TINY keys),
+// else the kind of job it becomes.
+template <class C>
+__device__ __forceinline__ uint32_t range_kind(unsigned long long m) {
+  return m <= (unsigned long long)C::TINY ? 0u : m <= (unsigned long long)C::TILE ? (uint32_t)JOB_LOCAL
+                                                                                  : (uint32_t)JOB_PART;
+}
+
+// Places a range of at most TINY keys whose keys sit in d (dir 1) or dn (dir 0): one key is
+// copied, more are sorted by the calling warp. Returns the number of keys placed.
+template <class C>
+__device__ unsigned long long place_small(const SortArgs<typename C::T>& a, uint32_t dir, unsigned long long s,
+                                          unsigned long long m, unsigned long long& tiny_keys) {
+  const int lane = threadIdx.x & 31;
+  const typename C::B* src = dir ? a.d : a.dn;
+  if (m == 0) return 0;
+  if (m == 1) {
+    if (!dir && lane == 0) a.d[s] = __ldcg(src + s);
+    return 1;
+  }
+  warp_sort_global<C>(src, a.d, s, (uint32_t)m);
+  tiny_keys += m;
+  return m;
+}
+
+// Decide what to do with a range whose keys sit in d (dir 1) or dn (dir 0).
 // Called by a whole warp. Returns the number of keys placed in their final position.
 template <class C>
 __device__ unsigned long long dispatch_range(const SortArgs<typename C::T>& a, uint32_t dir,
                                              unsigned long long s, unsigned long long e, uint32_t depth,
                                              unsigned long long& tiny_keys) {
   using B = typename C::B;
-  const int lane = threadIdx.x & 31;
   const unsigned long long m = e - s;
-  B* src = dir ? a.d : a.dn;
-  if (m == 0) return 0;
-  if (m == 1) {
-    if (!dir && lane == 0) a.d[s] = __ldcg(src + s);
-    return 1;
-  }
-  if (m <= (unsigned long long)C::TINY) {
-    warp_sort_global<C>(src, a.d, s, (uint32_t)m);
-    tiny_keys += m;
-    return m;
-  }
-  if (m <= (unsigned long long)C::TILE) {
+  const uint32_t kind = range_kind<C>(m);
+  if (!kind) return place_small<C>(a, dir, s, m, tiny_keys);
+  if (kind == JOB_LOCAL) {
     push_job<C>(a, JOB_LOCAL, dir, s, e, 0, depth);
     return 0;
   }
-  const B pv = sample_pivot_global<C, 4>(src, s, m);
+  const B pv = sample_pivot_global<C, 4>(dir ? a.d : a.dn, s, m);
   push_job<C>(a, JOB_PART, dir, s, e, (unsigned long long)pv, depth);
   return 0;
 }
@@ -617,49 +684,85 @@ struct Persistent {
     uint32_t failed = 0;
     Waiter idle(a.q);
     bool idling = false;
-    uint32_t tb = 0, next = kTake, resolved = 0;
+    // Tickets per grab: this CTA's share of the tickets waiting at the last grab, from one to
+    // kTake, so that a new job's chunks spread over all CTAs instead of queueing kTake deep on
+    // a few, while a deep queue is still taken kTake at a time (one atomic, and the tickets
+    // resolved in parallel lanes). At the
+    // frontier (the last grab ran past every ticket allocated so far) the producer takes its
+    // next ticket only once this CTA is idle, so that new work goes to CTAs that can start it
+    // at once rather than behind a local sort.
+    uint32_t tb = 0, take = 1, take_next = 1, next = 1, resolved = 0;
+    bool frontier = false;
     Ticket mine;
     mine.slot = 0;
     for (;;) {
       GQS_PROF_T(t0)
-      if (next == kTake) {  // take the next batch of tickets
-        uint32_t b = 0;
-        if (lane == 0) b = atomicAdd(&a.q->grab, kTake);
-        tb = __shfl_sync(0xffffffffu, b, 0);
-        next = 0;
-        resolved = 0;
-        ++nops;
-      }
-      if (!((resolved >> next) & 1u)) {
-        bool ok = false;
-        if (lane < (int)kTake && !((resolved >> lane) & 1u)) ok = resolve(a, tb + lane, mine);
-        resolved |= __ballot_sync(0xffffffffu, ok);
-      }
-      GQS_PROF_ADD(PF_P_GRAB, t0)
-      uint32_t kind;
-      if ((resolved >> next) & 1u) {
-        kind = __shfl_sync(0xffffffffu, mine.kind, next);  // job kinds double as item kinds
-        idling = false;
-      } else {
-        // The next ticket is not published yet: more work is coming, or the sort is over.
-        kind = ITEM_NONE;
-        if (lane == 0) {
-          GQS_PROF_T(t1)
-          if (ld_relaxed(&a.q->error) || ld_relaxed(&a.q->done) >= ld_relaxed(&a.q->total)) {
-            kind = ITEM_TERM;
-          } else if (need_flush) {
-            kind = ITEM_FLUSH;  // let the consumers finish what they hold before idling
-          } else {
-            if (!idling) {
-              idle = Waiter(a.q);
-              idling = true;
+      uint32_t kind = ITEM_NONE;
+      if (next == take) {
+        // need_flush is lane 0's; the branch below must be taken by the whole warp
+        if (frontier && __shfl_sync(0xffffffffu, need_flush ? 1u : 0u, 0) != 0u) {
+          kind = ITEM_FLUSH;  // hand the consumers their last chunk before waiting for idle
+        } else {  // take the next batch of tickets
+          uint32_t b = 0, ok = 1, fr = 0, nt = take_next;
+          if (lane == 0) {
+            if (frontier) {
+              // the most recent item released by the consumers, and the tile region free
+              if (k && !mbar_wait(&sm.empty[(k - 1) % C::STAGES], ((k - 1) / C::STAGES) & 1u, a.q, a.timeout_ns, 2))
+                ok = 0;
+              if (ok && nloc && !mbar_wait(&sm.lempty, (nloc - 1) & 1u, a.q, a.timeout_ns, 3)) ok = 0;
             }
-            if (!idle.step(a.q, a.timeout_ns, 1, true)) kind = ITEM_TERM;
+            if (ok) {
+              b = atomicAdd(&a.q->grab, take_next);
+              const uint32_t alloc_tickets = (uint32_t)ld_relaxed(&a.q->alloc);
+              const int avail = (int)(alloc_tickets - (b + take_next));
+              fr = avail < 0 ? 1u : 0u;
+              const int share = avail / (int)gridDim.x;  // this CTA's share of the waiting tickets
+              nt = share >= (int)kTake ? kTake : share > 1 ? (uint32_t)share : 1u;
+            }
           }
-          GQS_PROF_ADD(PF_P_IDLE, t1)
+          if (!__shfl_sync(0xffffffffu, ok, 0)) {
+            failed = 1;
+            break;
+          }
+          tb = __shfl_sync(0xffffffffu, b, 0);
+          take = take_next;
+          take_next = __shfl_sync(0xffffffffu, nt, 0);
+          frontier = __shfl_sync(0xffffffffu, fr, 0) != 0u;
+          next = 0;
+          resolved = 0;
+          ++nops;
         }
-        kind = __shfl_sync(0xffffffffu, kind, 0);
-        if (kind == ITEM_NONE) continue;
+      }
+      if (kind == ITEM_NONE) {
+        if (!((resolved >> next) & 1u)) {
+          bool ok = false;
+          if (lane < (int)take && !((resolved >> lane) & 1u)) ok = resolve(a, tb + lane, mine);
+          resolved |= __ballot_sync(0xffffffffu, ok);
+        }
+        GQS_PROF_ADD(PF_P_GRAB, t0)
+        if ((resolved >> next) & 1u) {
+          kind = __shfl_sync(0xffffffffu, mine.kind, next);  // job kinds double as item kinds
+          idling = false;
+        } else {
+          // The next ticket is not published yet: more work is coming, or the sort is over.
+          if (lane == 0) {
+            GQS_PROF_T(t1)
+            if (ld_relaxed(&a.q->error) || ld_relaxed(&a.q->done) >= ld_relaxed(&a.q->total)) {
+              kind = ITEM_TERM;
+            } else if (need_flush) {
+              kind = ITEM_FLUSH;  // let the consumers finish what they hold before idling
+            } else {
+              if (!idling) {
+                idle = Waiter(a.q);
+                idling = true;
+              }
+              if (!idle.step(a.q, a.timeout_ns, 1, true)) kind = ITEM_TERM;
+            }
+            GQS_PROF_ADD(PF_P_IDLE, t1)
+          }
+          kind = __shfl_sync(0xffffffffu, kind, 0);
+          if (kind == ITEM_NONE) continue;
+        }
       }
       const bool real = kind == ITEM_PART || kind == ITEM_LOCAL || kind == ITEM_FILL;
       const uint32_t src_lane = real ? next : 0u;
@@ -769,10 +872,23 @@ struct Persistent {
         push_job<C>(a, JOB_FILL, 0u, ss, se, (unsigned long long)pv, depth);
       }
     }
-    // Children live in this job's destination buffer; they are read the other way next.
+    // Children [js, ss) and [se, je) live in this job's destination buffer; they are read the
+    // other way next. Both pivots are sampled together and both jobs published with one
+    // allocation; children of at most TINY keys are sorted here, after the publication.
     const uint32_t cdir = dir ^ 1u;
-    placed += dispatch_range<C>(a, cdir, js, ss, depth + 1, st_tiny);
-    placed += dispatch_range<C>(a, cdir, se, je, depth + 1, st_tiny);
+    const uint32_t k0 = range_kind<C>(ss - js), k1 = range_kind<C>(je - se);
+    B p0 = 0, p1 = 0;
+    sample_pivots_global2<C, 4>(cdir ? a.d : a.dn, js, ss - js, k0 == JOB_PART, se, je - se, k1 == JOB_PART, p0,
+                                p1);
+    const uint32_t nj = (k0 ? 1u : 0u) + (k1 ? 1u : 0u);
+    if (nj) {
+      const uint32_t kinds[2] = {k0 ? k0 : k1, k1};
+      const unsigned long long cs[2] = {k0 ? js : se, se}, ce[2] = {k0 ? ss : je, je};
+      const unsigned long long cp[2] = {(unsigned long long)(k0 ? p0 : p1), (unsigned long long)p1};
+      push_jobs<C>(a, nj, kinds, cdir, cs, ce, cp, depth + 1);
+    }
+    if (!k0) placed += place_small<C>(a, cdir, js, ss - js, st_tiny);
+    if (!k1) placed += place_small<C>(a, cdir, se, je - se, st_tiny);
     if (lane == 0 && placed) atomicAdd(&a.q->done, placed);
     if (depth + 1 > st_depth) st_depth = depth + 1;
   }
