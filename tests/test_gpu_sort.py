@@ -252,3 +252,33 @@ def test_pipelined_host_sort(gpu_ctx, dtype, dist, n):
     assert np.array_equal(y.view(np.uint8), np.sort(x).view(np.uint8))
     st = gpu_ctx.stats()
     assert st["status"] == 0 and st["keys"] == n
+
+
+@pytest.mark.parametrize("dtype", ["u32", "f32", "f64"])
+def test_random_sizes_every_variant(dtype):
+    """Seeded stress of the job scheduling: every kernel variant sorts 30 arrays of random
+    log-uniform sizes in [1, 2^22] and random distributions, through the host and the device
+    entry points in turn; each result is bit-exact against numpy's sort (no NaN or -0.0)."""
+    torch = _torch()
+    tdt = {"u32": torch.int32, "f32": torch.float32, "f64": torch.float64}[dtype]
+    rng = np.random.default_rng(20260404)
+    for v in gqs_ctypes.variants(dtype):
+        ctx = gqs_ctypes.Context(variant=v["index"])
+        try:
+            for i in range(30):
+                n = int(np.exp(rng.uniform(0.0, np.log(1 << 22))))
+                dist = DISTS[dtype][int(rng.integers(len(DISTS[dtype])))]
+                a = gqs_ctypes.generate(dtype, dist, int(rng.integers(1 << 30)), n)
+                ref = np.sort(a)
+                if i % 2 == 0:
+                    b = a.copy()
+                    ctx.sort(b)
+                else:
+                    d = torch.from_numpy(a.view(np.int32) if dtype == "u32" else a).cuda()
+                    assert ctx.sort_dev(dtype, d.data_ptr(), None, n, torch.cuda.current_stream().cuda_stream) == 0
+                    b = d.cpu().numpy()
+                    b = b.view(np.uint32) if dtype == "u32" else b
+                assert np.array_equal(b.view(np.uint8), ref.view(np.uint8)), (v["name"], dist, n)
+                assert ctx.stats()["status"] == 0
+        finally:
+            ctx.close()
