@@ -1059,11 +1059,8 @@ struct Persistent {
       const B kk = Ops::key(keys[j]);
       const bool isl = kk < p, isg = kk > p;
       const uint32_t bl = __ballot_sync(0xffffffffu, isl), bg = __ballot_sync(0xffffffffu, isg);
-      if (isl || isg) {
-        B* const base = isl ? lbase : gbase;
-        const uint32_t o = isl ? lo + __popc(bl & ltm) : go + __popc(bg & ltm);
-        base[o] = keys[j];
-      }
+      const uint32_t r = __popc((isl ? bl : bg) & ltm);  // rank among the lanes of its side
+      if (isl || isg) (isl ? lbase + lo : gbase + go)[r] = keys[j];
       lo += __popc(bl);
       go += __popc(bg);
     }
