@@ -48,3 +48,28 @@ def test_cli_sorts_all_three_key_types(w, h):
                  "Average speedup over CPU std::sort:", "Using device 0:"):
         assert line in out
     assert f"Allocating array size of {w * h} (uint)" in out and f"Allocating array size of {w * h} (double)" in out
+
+
+SWEEP = os.path.join(ROOT, "gpu-quicksort_gb300", "cli", "sweep.sh")
+
+
+def test_sweep_script_stops_without_a_gb300():
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    assert subprocess.run(["bash", "-n", SWEEP]).returncode == 0
+    r = subprocess.run(["bash", SWEEP, "256", "1", "1"], stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True,
+                       timeout=120)
+    assert r.returncode != 0 and "Trial 1 ---- 256 x 256" in r.stdout and "no sm_103" in r.stdout
+
+
+@pytest.mark.gpu
+def test_sweep_script_small_sizes():
+    # count 256 and 512: 2^16, 2^17, 2^18 and 2^19 keys, one trial of two iterations each
+    r = subprocess.run(["bash", SWEEP, "512", "1", "2"], stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True,
+                       timeout=600)
+    assert r.returncode == 0, r.stdout[-2000:]
+    out = r.stdout
+    for w, h in ((256, 256), (512, 256), (512, 512), (1024, 512)):
+        assert f"---- {w} x {h} ----" in out and f"Allocating array size of {w * h} (float)" in out
+    assert out.count("verifying: true") == 4 * 3 * 2 and "verifying: false" not in out
