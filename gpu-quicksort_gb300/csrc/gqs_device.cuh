@@ -1286,7 +1286,30 @@ struct Persistent {
     }
     cbar();
     GQS_SPLIT_STAMP(9)
-    for (uint32_t i = tid; i < m; i += C::NC) {
+    // KU keys per thread in flight: their tree walks (one dependent shared load per level) and
+    // the scatter's atomic-then-store chains overlap (four 32-bit keys; two 64-bit keys, where
+    // four measured slower)
+    constexpr uint32_t KU = sizeof(B) == 4 ? 4u : 2u;
+    uint32_t i0 = tid;
+    for (; i0 + (KU - 1u) * (uint32_t)C::NC < m; i0 += KU * (uint32_t)C::NC) {
+      B k[KU];
+      uint32_t b[KU];
+#pragma unroll
+      for (uint32_t u = 0; u < KU; ++u) {
+        k[u] = A[i0 + u * (uint32_t)C::NC];
+        b[u] = 1u;
+      }
+      for (uint32_t l = 0; l < lg; ++l) {
+#pragma unroll
+        for (uint32_t u = 0; u < KU; ++u) b[u] = 2u * b[u] + (sm.spl[b[u]] < k[u] ? 1u : 0u);
+      }
+#pragma unroll
+      for (uint32_t u = 0; u < KU; ++u) {
+        sm.lb[i0 + u * (uint32_t)C::NC] = (uint8_t)(b[u] - nb);
+        atomicAdd(&sm.bcnt[b[u] - nb], 1u);
+      }
+    }
+    for (uint32_t i = i0; i < m; i += C::NC) {
       const B k = A[i];
       uint32_t b = 1u;
       for (uint32_t l = 0; l < lg; ++l) b = 2u * b + (sm.spl[b] < k ? 1u : 0u);
@@ -1326,7 +1349,15 @@ struct Persistent {
     }
     cbar();
     GQS_SPLIT_STAMP(11)
-    for (uint32_t i = tid; i < m; i += C::NC) {
+    uint32_t j0 = tid;
+    for (; j0 + (KU - 1u) * (uint32_t)C::NC < m; j0 += KU * (uint32_t)C::NC) {
+      uint32_t pos[KU];
+#pragma unroll
+      for (uint32_t u = 0; u < KU; ++u) pos[u] = atomicAdd(&sm.bcnt[sm.lb[j0 + u * (uint32_t)C::NC]], 1u);
+#pragma unroll
+      for (uint32_t u = 0; u < KU; ++u) sm.tileB[pos[u]] = A[j0 + u * (uint32_t)C::NC];
+    }
+    for (uint32_t i = j0; i < m; i += C::NC) {
       const uint32_t pos = atomicAdd(&sm.bcnt[sm.lb[i]], 1u);
       sm.tileB[pos] = A[i];
     }
