@@ -64,8 +64,21 @@ __global__ void __launch_bounds__(kThreads) merge_kernel(const typename KeyOps<T
   const size_t a0 = splits[blockIdx.x], a1 = splits[blockIdx.x + 1];
   const size_t b0 = d0 - a0, b1 = d1 - a1;
   const uint32_t la = (uint32_t)(a1 - a0), lb = (uint32_t)(b1 - b0), n = la + lb;
-  for (uint32_t i = threadIdx.x; i < la; i += kThreads) sa[i] = a[a0 + i];
-  for (uint32_t i = threadIdx.x; i < lb; i += kThreads) sa[la + i] = b[b0 + i];
+  {
+    // element i of the staged tile is a[a0 + i] for i < la, else b[b0 + i - la]; every thread
+    // issues all its loads before its first shared store, so they are in flight together
+    B v[kPer];
+#pragma unroll
+    for (int u = 0; u < kPer; ++u) {
+      const uint32_t i = threadIdx.x + (uint32_t)u * kThreads;
+      v[u] = i < la ? a[a0 + i] : (i < n ? b[b0 + (i - la)] : B(0));
+    }
+#pragma unroll
+    for (int u = 0; u < kPer; ++u) {
+      const uint32_t i = threadIdx.x + (uint32_t)u * kThreads;
+      if (i < n) sa[i] = v[u];
+    }
+  }
   __syncthreads();
   // this thread's outputs [o0, o1) of the tile: split the staged slices along the same path
   const uint32_t o0 = threadIdx.x * kPer < n ? threadIdx.x * kPer : n;
@@ -82,7 +95,11 @@ __global__ void __launch_bounds__(kThreads) merge_kernel(const typename KeyOps<T
     so[o] = take_a ? sa[i++] : sa[la + j++];
   }
   __syncthreads();
-  for (uint32_t k = threadIdx.x; k < n; k += kThreads) out[d0 + k] = so[k];
+#pragma unroll
+  for (int u = 0; u < kPer; ++u) {
+    const uint32_t k = threadIdx.x + (uint32_t)u * kThreads;
+    if (k < n) out[d0 + k] = so[k];
+  }
 }
 
 template <class T>
