@@ -63,6 +63,9 @@ constexpr int kMaxVariants = 16;
 // pieces, each sorted as soon as it has arrived, then the sorted pieces are merged.
 constexpr size_t kPipeMin = 1ull << 24;
 constexpr int kPieces = 4;
+// The last merge of a pipelined sort runs in kSlices launches; each slice of the result is copied
+// back while the next one is merged.
+constexpr int kSlices = 8;
 using gqs::cuda_status;
 using gqs::DeviceGuard;
 using gqs::job_capacity;
@@ -79,6 +82,7 @@ struct gqs_ctx {
   cudaStream_t stream = nullptr;       // used by the host-pointer calls
   cudaStream_t copy_stream = nullptr;  // host -> device pieces of a pipelined host sort
   cudaEvent_t ev_piece[4] = {};
+  cudaEvent_t ev_slice[8] = {};        // slices of a pipelined sort's last merge, done
   gqs::Queue* q_acc = nullptr;         // statistics of a pipelined sort, summed over its pieces
   void* merge_splits = nullptr;        // merge-path splits of the pipelined sort's merges
   size_t merge_splits_bytes = 0;
@@ -264,9 +268,10 @@ __global__ void accumulate_queue(const gqs::Queue* __restrict__ q, gqs::Queue* _
   }
 }
 
-// The host-pointer sort of a large array, overlapping the copy in with the sort: piece i is
-// copied on the copy stream while piece i - 1 is sorted; the sorted pieces are merged pairwise
-// (two merge passes for four pieces) and the result copied back. Lock held.
+// The host-pointer sort of a large array, overlapping the copies with the work: piece i is
+// copied in on the copy stream while piece i - 1 is sorted; the sorted pieces are merged
+// pairwise (two merge passes for four pieces), and the last merge runs in slices whose results
+// are copied back while the next slice is merged. Lock held.
 gqs_status sort_host_pipelined(gqs_ctx* c, int dtype, void* d, size_t n) {
   const size_t es = kElemSize[dtype];
   const size_t bytes = n * es;
@@ -300,14 +305,28 @@ gqs_status sort_host_pipelined(gqs_ctx* c, int dtype, void* d, size_t n) {
     accumulate_queue<<<1, 1, 0, c->stream>>>(c->q, c->q_acc);
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_status(e);
   }
-  // pieces 0+1 and 2+3 into the scratch, then the two halves back into pool_d
+  // pieces 0+1 and 2+3 into the scratch, then the two halves back into pool_d, in kSlices
+  // launches: each slice of the result goes back to the host on the copy stream while the
+  // next one is merged
+  static_assert(kSlices <= (int)(sizeof(c->ev_slice) / sizeof(c->ev_slice[0])), "one event per slice");
   e = gqs::merge_runs(dtype, dd, off[1], dd + off[1] * es, off[2] - off[1], dn, sp, c->stream);
   if (e == cudaSuccess)
     e = gqs::merge_runs(dtype, dd + off[2] * es, off[3] - off[2], dd + off[3] * es, off[4] - off[3], dn + off[2] * es,
                         sp, c->stream);
-  if (e == cudaSuccess) e = gqs::merge_runs(dtype, dn, off[2], dn + off[2] * es, n - off[2], dd, sp, c->stream);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(d, dd, bytes, cudaMemcpyDeviceToHost, c->stream);
-  if (e == cudaSuccess) e = cudaEventRecord(c->ev_done, c->stream);
+  const size_t nlo = off[2], nhi = n - off[2];
+  if (e == cudaSuccess) e = gqs::merge_plan(dtype, dn, nlo, dn + nlo * es, nhi, sp, c->stream);
+  const size_t tk = gqs::merge_tile_keys(), tiles = (n + tk - 1) / tk;
+  for (int sl = 0; sl < kSlices && e == cudaSuccess; ++sl) {
+    const size_t t0 = tiles * (size_t)sl / kSlices, t1 = tiles * (size_t)(sl + 1) / kSlices;
+    const size_t k0 = std::min(t0 * tk, n), k1 = std::min(t1 * tk, n);
+    e = gqs::merge_tiles(dtype, dn, nlo, dn + nlo * es, nhi, dd, sp, t0, t1, c->stream);
+    if (e == cudaSuccess) e = cudaEventRecord(c->ev_slice[sl], c->stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(c->copy_stream, c->ev_slice[sl], 0);
+    if (e == cudaSuccess && k1 > k0)
+      e = cudaMemcpyAsync(hd + k0 * es, dd + k0 * es, (k1 - k0) * es, cudaMemcpyDeviceToHost, c->copy_stream);
+  }
+  // the last copy follows every kernel of this call (it waited for the last slice)
+  if (e == cudaSuccess) e = cudaEventRecord(c->ev_done, c->copy_stream);
   if (e != cudaSuccess) return cuda_status(e);
   c->pending_acc = true;
   c->pending_timed = false;
@@ -532,6 +551,7 @@ gqs_status gqs_create(gqs_ctx** out, int device, const gqs_config* cfg) {
     }
     bool evs = true;
     for (cudaEvent_t& ev : c->ev_piece) evs = evs && cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) == cudaSuccess;
+    for (cudaEvent_t& ev : c->ev_slice) evs = evs && cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) == cudaSuccess;
     if (!evs) { st = GQS_ERR_CUDA; break; }
     if (cudaMalloc(&c->q_acc, sizeof(gqs::Queue)) != cudaSuccess) { st = GQS_ERR_NOMEM; break; }
     if (cudaEventCreate(&c->ev_begin) != cudaSuccess || cudaEventCreate(&c->ev_end) != cudaSuccess ||
@@ -576,6 +596,8 @@ void gqs_destroy(gqs_ctx* c) {
     if (c->stream) cudaStreamDestroy(c->stream);
     if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
     for (cudaEvent_t ev : c->ev_piece)
+      if (ev) cudaEventDestroy(ev);
+    for (cudaEvent_t ev : c->ev_slice)
       if (ev) cudaEventDestroy(ev);
     if (c->q_acc) cudaFree(c->q_acc);
     if (c->merge_splits) cudaFree(c->merge_splits);

@@ -65,8 +65,16 @@ VariantInfo variant_info(int dtype, int v);
 int variant_prepare(int dtype, int v);
 cudaError_t launch_sort(int dtype, const LaunchParams& p);
 // Merges sorted runs a[0, na) and b[0, nb) of key type dtype into out (defined in gqs_merge.cu);
-// `splits` is device scratch of merge_split_words(na + nb) words.
+// `splits` is device scratch of merge_split_words(na + nb) words. The output is made in tiles
+// of merge_tile_keys() keys: merge_plan finds where every tile starts in a and b, then
+// merge_tiles writes tiles [t0, t1) (several launches may cover the tiles in turn, so that
+// the first part of the output can leave while the rest is merged); merge_runs does both.
 size_t merge_split_words(size_t total);
+size_t merge_tile_keys();
+cudaError_t merge_plan(int dtype, const void* a, size_t na, const void* b, size_t nb, unsigned long long* splits,
+                       cudaStream_t s);
+cudaError_t merge_tiles(int dtype, const void* a, size_t na, const void* b, size_t nb, void* out,
+                        const unsigned long long* splits, size_t t0, size_t t1, cudaStream_t s);
 cudaError_t merge_runs(int dtype, const void* a, size_t na, const void* b, size_t nb, void* out,
                        unsigned long long* splits, cudaStream_t s);
 

@@ -52,16 +52,17 @@ template <class T>
 __global__ void __launch_bounds__(kThreads) merge_kernel(const typename KeyOps<T>::B* __restrict__ a, size_t na,
                                                          const typename KeyOps<T>::B* __restrict__ b, size_t nb,
                                                          const unsigned long long* __restrict__ splits,
-                                                         typename KeyOps<T>::B* __restrict__ out) {
+                                                         typename KeyOps<T>::B* __restrict__ out, size_t tile0) {
   using B = typename KeyOps<T>::B;
   using Ops = KeyOps<T>;
   __shared__ B sa[kTile];  // a slice, then b slice, packed: [0, la) and [la, la + lb)
   __shared__ B so[kTile];
   const size_t total = na + nb;
-  const size_t d0 = (size_t)blockIdx.x * kTile;
+  const size_t tile = tile0 + blockIdx.x;
+  const size_t d0 = tile * kTile;
   if (d0 >= total) return;
   const size_t d1 = d0 + kTile < total ? d0 + kTile : total;
-  const size_t a0 = splits[blockIdx.x], a1 = splits[blockIdx.x + 1];
+  const size_t a0 = splits[tile], a1 = splits[tile + 1];
   const size_t b0 = d0 - a0, b1 = d1 - a1;
   const uint32_t la = (uint32_t)(a1 - a0), lb = (uint32_t)(b1 - b0), n = la + lb;
   {
@@ -103,31 +104,59 @@ __global__ void __launch_bounds__(kThreads) merge_kernel(const typename KeyOps<T
 }
 
 template <class T>
-cudaError_t launch_merge(const void* a, size_t na, const void* b, size_t nb, void* out, unsigned long long* splits,
-                         cudaStream_t s) {
+cudaError_t launch_plan(const void* a, size_t na, const void* b, size_t nb, unsigned long long* splits,
+                        cudaStream_t s) {
   using B = typename KeyOps<T>::B;
   const size_t total = na + nb;
   if (total == 0) return cudaSuccess;
-  const size_t blocks = (total + kTile - 1) / kTile;
-  merge_splits<T><<<(unsigned)((blocks + 1 + 255) / 256), 256, 0, s>>>(
-      static_cast<const B*>(a), na, static_cast<const B*>(b), nb, splits, blocks + 1);
-  merge_kernel<T><<<(unsigned)blocks, kThreads, 0, s>>>(static_cast<const B*>(a), na, static_cast<const B*>(b), nb,
-                                                         splits, static_cast<B*>(out));
+  const size_t words = (total + kTile - 1) / kTile + 1;
+  merge_splits<T><<<(unsigned)((words + 255) / 256), 256, 0, s>>>(static_cast<const B*>(a), na,
+                                                                  static_cast<const B*>(b), nb, splits, words);
+  return cudaGetLastError();
+}
+
+template <class T>
+cudaError_t launch_tiles(const void* a, size_t na, const void* b, size_t nb, void* out,
+                         const unsigned long long* splits, size_t t0, size_t t1, cudaStream_t s) {
+  using B = typename KeyOps<T>::B;
+  const size_t tiles = (na + nb + kTile - 1) / kTile;
+  if (t1 > tiles) t1 = tiles;
+  if (t0 >= t1) return cudaSuccess;
+  merge_kernel<T><<<(unsigned)(t1 - t0), kThreads, 0, s>>>(static_cast<const B*>(a), na, static_cast<const B*>(b), nb,
+                                                          splits, static_cast<B*>(out), t0);
   return cudaGetLastError();
 }
 
 }  // namespace
 
 size_t merge_split_words(size_t total) { return (total + kTile - 1) / kTile + 1; }
+size_t merge_tile_keys() { return kTile; }
+
+cudaError_t merge_plan(int dtype, const void* a, size_t na, const void* b, size_t nb, unsigned long long* splits,
+                       cudaStream_t s) {
+  switch (dtype) {
+    case DT_U32: return launch_plan<uint32_t>(a, na, b, nb, splits, s);
+    case DT_F32: return launch_plan<float>(a, na, b, nb, splits, s);
+    case DT_F64: return launch_plan<double>(a, na, b, nb, splits, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+cudaError_t merge_tiles(int dtype, const void* a, size_t na, const void* b, size_t nb, void* out,
+                        const unsigned long long* splits, size_t t0, size_t t1, cudaStream_t s) {
+  switch (dtype) {
+    case DT_U32: return launch_tiles<uint32_t>(a, na, b, nb, out, splits, t0, t1, s);
+    case DT_F32: return launch_tiles<float>(a, na, b, nb, out, splits, t0, t1, s);
+    case DT_F64: return launch_tiles<double>(a, na, b, nb, out, splits, t0, t1, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
 
 cudaError_t merge_runs(int dtype, const void* a, size_t na, const void* b, size_t nb, void* out,
                        unsigned long long* splits, cudaStream_t s) {
-  switch (dtype) {
-    case DT_U32: return launch_merge<uint32_t>(a, na, b, nb, out, splits, s);
-    case DT_F32: return launch_merge<float>(a, na, b, nb, out, splits, s);
-    case DT_F64: return launch_merge<double>(a, na, b, nb, out, splits, s);
-    default: return cudaErrorInvalidValue;
-  }
+  cudaError_t e = merge_plan(dtype, a, na, b, nb, splits, s);
+  if (e == cudaSuccess) e = merge_tiles(dtype, a, na, b, nb, out, splits, 0, merge_split_words(na + nb), s);
+  return e;
 }
 
 }  // namespace gqs
