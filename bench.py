@@ -382,6 +382,10 @@ def run_serve(args, gqs_ctypes):
     rate = args.serve_load * sat_b["keys_per_s"] / mean_keys
     poi_b, _ = run_serve_arm(gqs_ctypes, templates, stream, False, rate, pool)
     poi_p, _ = run_serve_arm(gqs_ctypes, templates, stream, True, rate, pool)
+    # the same stream at the per-request server's own load point, which both modes sustain
+    rate_p = args.serve_load * sat_p["keys_per_s"] / mean_keys
+    low_b, _ = run_serve_arm(gqs_ctypes, templates, stream, False, rate_p, pool)
+    low_p, _ = run_serve_arm(gqs_ctypes, templates, stream, True, rate_p, pool)
     # bit-exact checks on the sampled requests: both modes, against numpy's sort of the input
     ok = True
     for i, a in samp_b.items():
@@ -409,6 +413,9 @@ def run_serve(args, gqs_ctypes):
                        "batched_arena_peak_gb": sat_b["arena_peak_gb"]},
         "poisson": {"offered_load": f"{args.serve_load:.2f} x batched capacity", "rate_req_s": rate,
                     "offered_gkeys_s": rate * mean_keys / 1e9, "batched": lat(poi_b), "per_request": lat(poi_p)},
+        "poisson_per_request_load": {"offered_load": f"{args.serve_load:.2f} x per-request capacity",
+                                     "rate_req_s": rate_p, "offered_gkeys_s": rate_p * mean_keys / 1e9,
+                                     "batched": lat(low_b), "per_request": lat(low_p)},
         "check": {"sampled_requests": len(samp_b), "bit_exact_vs_numpy_and_per_request": ok},
     }
 
