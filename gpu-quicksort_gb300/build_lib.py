@@ -2,6 +2,8 @@
 
     libgqs.so           the CUDA sort library behind include/gqs.h (sm_103a only)
     libgqs_workload.so  seeded synthetic workload generators (host C++)
+    libgqs_prof.so      on request (profile=True): the library with per-role cycle counters
+    libgqs_check.so     on request (check=True): the library with device bounds checks
 
 Objects go to _build/ next to this file; the libraries land beside this file.
 Run as a script or call build().
@@ -29,6 +31,7 @@ VARIANT_TU = "gqs_variant_tu.cu"  # compiled once per (key type, variant index)
 
 LIB = os.path.join(HERE, "libgqs.so")
 PROF_LIB = os.path.join(HERE, "libgqs_prof.so")  # -DGQS_PROFILE: per-role cycle counters
+CHECK_LIB = os.path.join(HERE, "libgqs_check.so")  # -DGQS_CHECK: bounds checks on the device
 WORKLOAD_LIB = os.path.join(HERE, "libgqs_workload.so")
 CLI = os.path.join(HERE, "quicksort")  # the reference-compatible benchmark command line
 
@@ -79,12 +82,15 @@ def _units() -> list[tuple[str, str, list[str]]]:
     return units
 
 
-def build(force: bool = False, verbose: bool = False, profile: bool = False) -> dict:
+def build(force: bool = False, verbose: bool = False, profile: bool = False, check: bool = False) -> dict:
     """Compiles what is out of date; returns the library paths. profile=True builds
-    libgqs_prof.so with the device cycle counters instead of libgqs.so."""
-    bdir = BUILD + ("_prof" if profile else "")
-    lib = PROF_LIB if profile else LIB
-    extra = ["-DGQS_PROFILE"] if profile else []
+    libgqs_prof.so with the device cycle counters, check=True libgqs_check.so with the device
+    bounds checks, instead of libgqs.so."""
+    if profile and check:
+        raise ValueError("one library flavour at a time")
+    bdir = BUILD + ("_prof" if profile else "_check" if check else "")
+    lib = PROF_LIB if profile else CHECK_LIB if check else LIB
+    extra = ["-DGQS_PROFILE"] if profile else ["-DGQS_CHECK"] if check else []
     os.makedirs(bdir, exist_ok=True)
     nvcc = _nvcc()
     headers = _headers()
@@ -112,7 +118,7 @@ def build(force: bool = False, verbose: bool = False, profile: bool = False) -> 
         _run([nvcc] + ARCH + ["-shared", "-o", lib] + objs + ["-Xcompiler", "-fPIC"])
     out = {"lib": lib, "workload": WORKLOAD_LIB}
     csrc = os.path.join(HERE, "cli", "quicksort_main.cpp")
-    if not profile and os.path.exists(csrc):
+    if not profile and not check and os.path.exists(csrc):
         if force or _stale(CLI, [csrc, LIB, WORKLOAD_LIB, os.path.join(INCLUDE, "gqs.h")]):
             _run([nvcc, "-O2", "-std=c++17", "-I" + INCLUDE, "-I" + os.path.join(HERE, "workload"), csrc,
                   "-L" + HERE, "-lgqs", "-lgqs_workload", "-Xlinker", "-rpath,$ORIGIN", "-o", CLI])
@@ -123,4 +129,4 @@ def build(force: bool = False, verbose: bool = False, profile: bool = False) -> 
 
 
 if __name__ == "__main__":
-    build(force="--force" in sys.argv, verbose=True, profile="--profile" in sys.argv)
+    build(force="--force" in sys.argv, verbose=True, profile="--profile" in sys.argv, check="--check" in sys.argv)

@@ -155,7 +155,7 @@ gqs_status wait_pending_locked(gqs_ctx* c) {
 
 // Validates, grows pools, and enqueues one sort on `stream`. Caller holds the lock.
 gqs_status enqueue_locked(gqs_ctx* c, int dtype, void* d, void* dn, size_t n, const unsigned long long* offsets,
-                          size_t nseg, cudaStream_t stream) {
+                          size_t nseg, cudaStream_t stream, unsigned long long check_n = 0) {
   const size_t es = kElemSize[dtype];
   if (!d || (reinterpret_cast<uintptr_t>(d) % es) != 0) return GQS_ERR_INVALID;
   if (dn && (reinterpret_cast<uintptr_t>(dn) % es) != 0) return GQS_ERR_INVALID;
@@ -225,6 +225,7 @@ gqs_status enqueue_locked(gqs_ctx* c, int dtype, void* d, void* dn, size_t n, co
   p.stream = stream;
   p.ev_begin = c->cfg.timing ? c->ev_begin : nullptr;
   p.ev_end = c->cfg.timing ? c->ev_end : nullptr;
+  p.check_n = check_n;
   e = gqs::launch_sort(dtype, p);
   if (e != cudaSuccess) return cuda_status(e);
   e = cudaEventRecord(c->ev_done, stream);
@@ -758,6 +759,22 @@ gqs_status gqs_selftest_stalled_queue(gqs_ctx* c, int dtype, uint32_t timeout_ms
   return wait_pending_locked(c);
 }
 
+gqs_status gqs_selftest_bounds(gqs_ctx* c, int dtype) {
+  if (!c || dtype < 0 || dtype > 2) return GQS_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(c->mu);
+  DeviceGuard dg(c->device);
+  const size_t n = 1u << 16, es = kElemSize[dtype];
+  (void)wait_pending_locked(c);
+  gqs_status st = grow(&c->pool_d, &c->pool_d_bytes, n * es);
+  if (st != GQS_OK) return st;
+  // equal keys (0x5a bytes: an ordinary value for every key type); any keys would do
+  cudaError_t e = cudaMemsetAsync(c->pool_d, 0x5a, n * es, c->stream);
+  if (e != cudaSuccess) return cuda_status(e);
+  st = enqueue_locked(c, dtype, c->pool_d, nullptr, n, nullptr, 1, c->stream, n / 2);
+  if (st != GQS_OK) return st;
+  return wait_pending_locked(c);
+}
+
 gqs_status gqs_sync(gqs_ctx* c) {
   if (!c) return GQS_ERR_INVALID;
   std::lock_guard<std::mutex> lk(c->mu);
@@ -825,6 +842,7 @@ const char* gqs_strerror(gqs_status s) {
     case GQS_ERR_NO_DEVICE: return "no sm_103 CUDA device";
     case GQS_ERR_INTERNAL: return "internal error";
     case GQS_ERR_CANCELLED: return "request cancelled";
+    case GQS_ERR_BOUNDS: return "an index or record outside the sort's bounds (check build)";
   }
   return "unknown status";
 }

@@ -29,7 +29,7 @@ namespace gqs {
 
 // ---------------------------------------------------------------------------
 // Status codes written by the kernels (the C ABI uses the same numbers).
-enum : uint32_t { ST_OK = 0, ST_INVALID = 1, ST_TIMEOUT = 4, ST_CAPACITY = 5, ST_INTERNAL = 7 };
+enum : uint32_t { ST_OK = 0, ST_INVALID = 1, ST_TIMEOUT = 4, ST_CAPACITY = 5, ST_INTERNAL = 7, ST_BOUNDS = 9 };
 
 enum : uint32_t { JOB_PART = 1, JOB_LOCAL = 2, JOB_FILL = 3 };
 enum : uint32_t { ITEM_PART = 1, ITEM_LOCAL = 2, ITEM_FILL = 3, ITEM_TERM = 4, ITEM_FLUSH = 5, ITEM_NONE = 6 };
@@ -158,6 +158,7 @@ struct SortArgs {
   uint32_t capacity;         // job records
   uint32_t tmask;            // ticket ring size - 1 (a power of two)
   unsigned long long timeout_ns;
+  unsigned long long n;      // every key index of the sort is below n (checked by -DGQS_CHECK builds)
 };
 
 // Kernel configuration. TILE keys fit one local (on-chip) sort; CHUNK keys are one staged
@@ -215,6 +216,9 @@ struct Desc {
   unsigned long long gbeg;  // first element (global index) of the staged range
   unsigned long long pivot;
   uint32_t len, off, job, kind, dir, pad;
+#ifdef GQS_CHECK
+  unsigned long long jlo, jhi;  // the job's range: every key this item writes stays inside it
+#endif
 };
 
 template <class C>
@@ -247,6 +251,20 @@ struct alignas(128) Smem {
 __device__ __forceinline__ void set_error(Queue* q, uint32_t code, unsigned long long info) {
   if (atomicCAS(&q->error, 0u, code) == 0u) q->error_info = info;
 }
+
+// Debug builds (-DGQS_CHECK) test every job record, staged range and global write index
+// against the sort's bounds; a failed test records ST_BOUNDS with the site's code in
+// error_info, the access is skipped, and every role then winds down through its error path.
+// Product builds compile the tests out.
+#ifdef GQS_CHECK
+#define GQS_OK(cond, q, code) ((cond) || (set_error((q), ST_BOUNDS, (code)), false))
+#define GQS_CHECK_PARAMS , unsigned long long chk_lo, unsigned long long chk_hi, Queue* chk_q
+#define GQS_CHECK_ARGS(lo, hi, q) , (lo), (hi), (q)
+#else
+#define GQS_OK(cond, q, code) true
+#define GQS_CHECK_PARAMS
+#define GQS_CHECK_ARGS(lo, hi, q)
+#endif
 
 __device__ __forceinline__ unsigned long long progress_word(Queue* q) {
   return ld_relaxed(&q->done) + ld_relaxed(&q->alloc) * 0x9E3779B97F4A7C15ull +
@@ -423,6 +441,9 @@ __device__ bool push_jobs(const SortArgs<typename C::T>& a, uint32_t njobs, cons
     if ((unsigned long long)slot + njobs > a.capacity || untaken > (long long)a.tmask + 1) {
       set_error(a.q, ST_CAPACITY, slot);
       ok = 0;
+    } else if (!GQS_OK(start[0] <= end[0] && end[0] <= a.n && (njobs < 2 || (start[1] <= end[1] && end[1] <= a.n)),
+                       a.q, 0xB001ull)) {
+      ok = 0;
     } else {
 #pragma unroll
       for (int i = 0; i < 2; ++i) {
@@ -552,6 +573,7 @@ __device__ unsigned long long place_small(const SortArgs<typename C::T>& a, uint
   const int lane = threadIdx.x & 31;
   const typename C::B* src = dir ? a.d : a.dn;
   if (m == 0) return 0;
+  if (!GQS_OK(s + m <= a.n, a.q, 0xB002ull)) return 0;
   if (m == 1) {
     if (!dir && lane == 0) a.d[s] = __ldcg(src + s);
     return 1;
@@ -645,6 +667,7 @@ struct Persistent {
     const unsigned long long e = ld_acquire(a.tmap + (t & a.tmask));
     if ((uint32_t)(e >> 32) != t + 1u) return false;
     const uint32_t slot = (uint32_t)e;
+    if (!GQS_OK(slot < a.capacity, a.q, 0xB003ull)) return false;
     const Job* j = a.jobs + slot;
     tk.slot = slot;
     tk.kind = __ldcg(&j->kind);
@@ -654,6 +677,8 @@ struct Persistent {
     tk.pivot = __ldcg(&j->pivot);
     tk.grid = __ldcg(&j->grid);
     tk.chunk = t - __ldcg(&j->t0);
+    if (!GQS_OK(tk.kind >= JOB_PART && tk.kind <= JOB_FILL && tk.js <= tk.je && tk.je <= a.n, a.q, 0xB004ull))
+      return false;
     return true;
   }
 
@@ -800,7 +825,13 @@ struct Persistent {
             const unsigned long long ce = ce0 < je ? ce0 : je;
             dd.gbeg = cs;
             dd.len = (uint32_t)(ce - cs);
-            if (kind == ITEM_PART) {
+#ifdef GQS_CHECK
+            dd.jlo = js;
+            dd.jhi = je;
+#endif
+            if (!GQS_OK(cs < ce && ce - cs <= (unsigned long long)grain, a.q, 0xB005ull)) {
+              failed = 1;  // nothing staged; the whole warp leaves the loop below
+            } else if (kind == ITEM_PART) {
               dd.off = stage_range(src, cs, ce, sm.stage[s], &sm.full[s]);
               need_flush = true;
             } else {
@@ -812,7 +843,7 @@ struct Persistent {
             GQS_PROF_T(t4)
             const bool free_tile = mbar_wait(&sm.lempty, (nloc & 1u) ^ 1u, a.q, a.timeout_ns, 3);
             GQS_PROF_ADD(PF_P_LEMPTY, t4)
-            if (!free_tile) {
+            if (!free_tile || !GQS_OK(je - js <= (unsigned long long)C::TILE, a.q, 0xB006ull)) {
               failed = 1;
             } else {
               dd.gbeg = js;
@@ -857,6 +888,7 @@ struct Persistent {
     const unsigned long long ss = __ldcg(&j->sstart), se = __ldcg(&j->send);
     const B pv = (B)__ldcg(&j->pivot);
     const uint32_t dir = __ldcg(&j->dir), depth = __ldcg(&j->depth);
+    if (!GQS_OK(js <= ss && ss <= se && se <= je && je <= a.n, a.q, 0xB00Aull)) return;
     unsigned long long placed = 0;
     // Pivot run [ss, se) -> d (the reference's last block writes it serially,
     // QuicksortKernels.cl:214-216; here a warp writes short runs and long runs become
@@ -1038,7 +1070,7 @@ struct Persistent {
   // pivot run. (gqsort_kernel pass 2, QuicksortKernels.cl:190-203.)
   static __device__ __forceinline__ void scatter_chunk(const B (&keys)[C::KPT], B p, B* dst, unsigned long long lb,
                                                        unsigned long long gb, const uint32_t* wlt,
-                                                       const uint32_t* wgt) {
+                                                       const uint32_t* wgt GQS_CHECK_PARAMS) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     uint32_t vl = lane < C::NCW ? wlt[lane] : 0u, vg = lane < C::NCW ? wgt[lane] : 0u;
     uint32_t il = vl, ig = vg;
@@ -1060,7 +1092,15 @@ struct Persistent {
       const bool isl = kk < p, isg = kk > p;
       const uint32_t bl = __ballot_sync(0xffffffffu, isl), bg = __ballot_sync(0xffffffffu, isg);
       const uint32_t r = __popc((isl ? bl : bg) & ltm);  // rank among the lanes of its side
+#ifdef GQS_CHECK
+      B* const to = (isl ? lbase + lo : gbase + go) + r;
+      const unsigned long long ix = (unsigned long long)(to - dst);
+      const bool inside = !(isl || isg) || GQS_OK(ix >= chk_lo && ix < chk_hi, chk_q, 0xB007ull);
+      if ((isl || isg) && inside) *to = keys[j];
+#else
+      // (this exact form: computing the address outside the branch measured 6 % slower)
       if (isl || isg) (isl ? lbase + lo : gbase + go)[r] = keys[j];
+#endif
       lo += __popc(bl);
       go += __popc(bg);
     }
@@ -1355,11 +1395,12 @@ struct Persistent {
 #pragma unroll
       for (uint32_t u = 0; u < KU; ++u) pos[u] = atomicAdd(&sm.bcnt[sm.lb[j0 + u * (uint32_t)C::NC]], 1u);
 #pragma unroll
-      for (uint32_t u = 0; u < KU; ++u) sm.tileB[pos[u]] = A[j0 + u * (uint32_t)C::NC];
+      for (uint32_t u = 0; u < KU; ++u)
+        if (GQS_OK(pos[u] < m, a.q, 0xB00Bull)) sm.tileB[pos[u]] = A[j0 + u * (uint32_t)C::NC];
     }
     for (uint32_t i = j0; i < m; i += C::NC) {
       const uint32_t pos = atomicAdd(&sm.bcnt[sm.lb[i]], 1u);
-      sm.tileB[pos] = A[i];
+      if (GQS_OK(pos < m, a.q, 0xB00Bull)) sm.tileB[pos] = A[i];
     }
     cbar();
     GQS_SPLIT_STAMP(12)
@@ -1460,6 +1501,9 @@ struct Persistent {
     uint32_t pend_len = 0, pend_job = 0, pend_par = 0, scat_job = 0;
     B pend_p = 0;
     B* pend_dst = nullptr;
+#ifdef GQS_CHECK
+    unsigned long long pend_lo = 0, pend_hi = 0;
+#endif
     unsigned long long st_part = 0, st_local = 0, st_chunks = 0;
     uint32_t st_local_jobs = 0, st_fill_jobs = 0;
     GQS_PROF_DECL
@@ -1547,7 +1591,8 @@ struct Persistent {
         have_scat = false;
         if (have_pend) {
           const uint32_t e = (npart - 1) % C::RQ;
-          scatter_chunk(pend, pend_p, pend_dst, sm.rs_lb[e], sm.rs_gb[e], sm.wlt[pend_par], sm.wgt[pend_par]);
+          scatter_chunk(pend, pend_p, pend_dst, sm.rs_lb[e], sm.rs_gb[e], sm.wlt[pend_par],
+                        sm.wgt[pend_par] GQS_CHECK_ARGS(pend_lo, pend_hi, a.q));
           have_scat = true;
           scat_job = pend_job;
         }
@@ -1559,6 +1604,10 @@ struct Persistent {
         pend_par = par;
         pend_p = p;
         pend_dst = dd.dir ? a.dn : a.d;
+#ifdef GQS_CHECK
+        pend_lo = dd.jlo;
+        pend_hi = dd.jhi;
+#endif
         have_pend = true;
         st_part += dd.len;
         ++st_chunks;
@@ -1577,7 +1626,8 @@ struct Persistent {
       if (!sm.cons_ok) break;
       if (have_pend) {
         const uint32_t e = (npart - 1) % C::RQ;
-        scatter_chunk(pend, pend_p, pend_dst, sm.rs_lb[e], sm.rs_gb[e], sm.wlt[pend_par], sm.wgt[pend_par]);
+        scatter_chunk(pend, pend_p, pend_dst, sm.rs_lb[e], sm.rs_gb[e], sm.wlt[pend_par],
+                      sm.wgt[pend_par] GQS_CHECK_ARGS(pend_lo, pend_hi, a.q));
       }
       cbar();
       if (tid == 0) {
@@ -1594,7 +1644,8 @@ struct Persistent {
         GQS_PROF_T(tf)
         const B raw = Ops::raw((B)dd.pivot);
         B* out = a.d + dd.gbeg;
-        for (uint32_t i = tid; i < dd.len; i += C::NC) out[i] = raw;
+        const uint32_t flen = GQS_OK(dd.gbeg + dd.len <= a.n, a.q, 0xB008ull) ? dd.len : 0u;
+        for (uint32_t i = tid; i < flen; i += C::NC) out[i] = raw;
         ++st_fill_jobs;
         GQS_PROF_ADD(PF_C_FILL, tf)
         if (tid == 0) atomicAdd(&a.q->done, (unsigned long long)dd.len);
@@ -1636,8 +1687,9 @@ struct Persistent {
         // Write the sorted tile to d: one bulk TMA store for the 16-byte-aligned body,
         // plain stores for the ragged ends (a bulk store must not touch bytes outside).
         B* out = a.d + dd.gbeg;
+        const uint32_t mw = GQS_OK(dd.gbeg + m <= a.n, a.q, 0xB009ull) ? m : 0u;  // keys written
         const uintptr_t olo = reinterpret_cast<uintptr_t>(out);
-        const uintptr_t ohi = reinterpret_cast<uintptr_t>(out + m);
+        const uintptr_t ohi = reinterpret_cast<uintptr_t>(out + mw);
         const uintptr_t ga = (olo + 15) & ~uintptr_t(15), gb = ohi & ~uintptr_t(15);
         const uint32_t head = (uint32_t)((ga - olo) / sizeof(B));
         const bool tma_ok = ga < gb && ((smem_addr(A + head) & 15u) == 0u);
@@ -1650,11 +1702,11 @@ struct Persistent {
             bulk_commit();
           }
           for (uint32_t i = tid; i < head; i += C::NC) out[i] = A[i];
-          for (uint32_t i = tail0 + tid; i < m; i += C::NC) out[i] = A[i];
+          for (uint32_t i = tail0 + tid; i < mw; i += C::NC) out[i] = A[i];
           if (tid == 0) bulk_wait_read_all();
         } else {
           cbar();
-          for (uint32_t i = tid; i < m; i += C::NC) out[i] = A[i];
+          for (uint32_t i = tid; i < mw; i += C::NC) out[i] = A[i];
         }
         cbar();  // every read of the tile is done before the producer may refill it
         if (tid == 0) {

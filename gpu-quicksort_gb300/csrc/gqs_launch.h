@@ -44,6 +44,7 @@ struct LaunchParams {
   cudaStream_t stream;
   cudaEvent_t ev_begin;  // optional: recorded around the persistent kernel
   cudaEvent_t ev_end;
+  unsigned long long check_n;  // 0, or a tighter bound on key indices for -DGQS_CHECK builds' tests
 };
 
 // Per key type (defined in gqs_sort_dispatch.cu).

@@ -42,6 +42,7 @@ struct VariantOps {
     a.capacity = p.capacity;
     a.tmask = p.tmask;
     a.timeout_ns = p.timeout_ns;
+    a.n = p.check_n ? p.check_n : p.n;
     const uint32_t nseg = p.offsets ? p.nseg : 1u;
     const uint32_t seed_blocks = (nseg + 7u) / 8u;  // 8 warps per 256-thread block, one per segment
     seed_kernel<C><<<seed_blocks, 256, 0, p.stream>>>(a, p.offsets, p.nseg_dev, nseg, p.n, p.pairs);

@@ -21,7 +21,8 @@ DIST = {"uniform": 0, "sorted": 1, "reverse": 2, "distinct16": 3, "zipf": 4, "ga
         "allequal": 7}
 
 STATUS = {0: "GQS_OK", 1: "GQS_ERR_INVALID", 2: "GQS_ERR_CUDA", 3: "GQS_ERR_NOMEM", 4: "GQS_ERR_TIMEOUT",
-          5: "GQS_ERR_CAPACITY", 6: "GQS_ERR_NO_DEVICE", 7: "GQS_ERR_INTERNAL", 8: "GQS_ERR_CANCELLED"}
+          5: "GQS_ERR_CAPACITY", 6: "GQS_ERR_NO_DEVICE", 7: "GQS_ERR_INTERNAL", 8: "GQS_ERR_CANCELLED",
+          9: "GQS_ERR_BOUNDS"}
 
 # Every function include/gqs.h declares.
 EXPORTS = [
@@ -37,6 +38,7 @@ EXPORTS = [
     "gqs_srv_config_default", "gqs_srv_create", "gqs_srv_destroy", "gqs_srv_submit", "gqs_srv_wait",
     "gqs_srv_wait_any", "gqs_srv_cancel", "gqs_srv_drain", "gqs_srv_stats", "gqs_srv_now_ns",
     "gqs_selftest_stalled_queue",
+    "gqs_selftest_bounds",
     "gqs_sort_pairs_u32", "gqs_sort_pairs_f32", "gqs_sort_pairs_u32_dev", "gqs_sort_pairs_f32_dev",
 ]
 
@@ -194,6 +196,8 @@ def load_library(path: str | None = None) -> C.CDLL:
     lib.gqs_srv_cancel.restype = st
     lib.gqs_selftest_stalled_queue.argtypes = [vp, C.c_int, C.c_uint32]
     lib.gqs_selftest_stalled_queue.restype = st
+    lib.gqs_selftest_bounds.argtypes = [vp, C.c_int]
+    lib.gqs_selftest_bounds.restype = st
     lib.gqs_srv_drain.argtypes = [vp]
     lib.gqs_srv_drain.restype = st
     lib.gqs_srv_stats.argtypes = [vp, C.POINTER(ServerStats)]
@@ -313,6 +317,11 @@ class Context:
 
     def set_variant(self, dtype: str, v: int) -> None:
         _check(self.lib.gqs_set_variant(self.h, DTYPES[dtype], v), "gqs_set_variant")
+
+    def selftest_bounds(self, dtype: str) -> int:
+        """Sorts keys under a deliberately short index bound; a -DGQS_CHECK build reports
+        GQS_ERR_BOUNDS, the product build sorts them (GQS_OK)."""
+        return self.lib.gqs_selftest_bounds(self.h, DTYPES[dtype])
 
     def selftest_stalled_queue(self, dtype: str, timeout_ms: int) -> int:
         """Runs the kernel on a queue that can never finish; returns the status it reports."""

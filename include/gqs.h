@@ -41,7 +41,9 @@ typedef enum gqs_status {
   GQS_ERR_CAPACITY = 5,  /* the device job queue overflowed (pathological pivot sequence) */
   GQS_ERR_NO_DEVICE = 6, /* no usable CUDA device, or not an sm_103 GPU */
   GQS_ERR_INTERNAL = 7,  /* an internal invariant failed on the device */
-  GQS_ERR_CANCELLED = 8  /* a server request was cancelled before it ran */
+  GQS_ERR_CANCELLED = 8, /* a server request was cancelled before it ran */
+  GQS_ERR_BOUNDS = 9     /* a -DGQS_CHECK build found a job record, range or write index outside
+                            the sort's bounds (and skipped the access) */
 } gqs_status;
 
 typedef enum gqs_dtype { GQS_U32 = 0, GQS_F32 = 1, GQS_F64 = 2 } gqs_dtype;
@@ -267,6 +269,13 @@ uint64_t gqs_srv_now_ns(void);
  * or hang is involved; the context stays usable. No reference counterpart (the reference waits
  * on the host with blocking reads). */
 gqs_status gqs_selftest_stalled_queue(gqs_ctx* ctx, int dtype, uint32_t timeout_ms);
+
+/* Self-test of the bounds checks of a -DGQS_CHECK build (libgqs_check.so): sorts 2^16 keys of
+ * type `dtype` in the context's pool while telling the kernel that key indices end at 2^15, so
+ * the first job already lies outside the bound. A check build reports GQS_ERR_BOUNDS without
+ * touching anything past the bound; the product build, whose checks are compiled out, sorts the
+ * keys and returns GQS_OK. Every access stays inside the 2^16-key buffers either way. */
+gqs_status gqs_selftest_bounds(gqs_ctx* ctx, int dtype);
 
 /* Waits for the context's last enqueued sort and returns its device status. */
 gqs_status gqs_sync(gqs_ctx* ctx);
