@@ -789,6 +789,7 @@ def main():
         "passes_per_key": (stats_last["part_keys"] + stats_last["local_keys"] + stats_last["tiny_keys"]) / n,
         "serve": serve,
         "profile": ctx.profile() if args.profile else None,
+        "levels": ctx.levels() if args.profile else None,
         "wall_s": wall,
     }
     print(json.dumps(line), flush=True)

@@ -112,6 +112,10 @@ struct gqs_ctx {
   unsigned long long pending_keys = 0;
   gqs_stats last{};
   uint64_t last_prof[32] = {};
+#ifdef GQS_PROFILE
+  unsigned long long last_lvl[gqs::kLevels][6] = {};  // per-level rows of the last sort
+  unsigned long long last_lvl_start = 0;
+#endif
   int variant[4] = {0, 0, 0, 0};  // per key type, and the internal packed pairs
   int blocks_per_sm[4][kMaxVariants] = {};
 };
@@ -150,6 +154,10 @@ gqs_status wait_pending_locked(gqs_ctx* c) {
   }
   c->last = s;
   for (int i = 0; i < 32; ++i) c->last_prof[i] = c->q_host->prof[i];
+#ifdef GQS_PROFILE
+  std::memcpy(c->last_lvl, c->q_host->lvl, sizeof(c->last_lvl));
+  c->last_lvl_start = c->q_host->lvl_start;
+#endif
   return (gqs_status)s.status;
 }
 
@@ -267,6 +275,14 @@ __global__ void accumulate_queue(const gqs::Queue* __restrict__ q, gqs::Queue* _
     acc->error = q->error;
     acc->error_info = q->error_info;
   }
+#ifdef GQS_PROFILE
+  if (!acc->lvl_start || (q->lvl_start && q->lvl_start < acc->lvl_start)) acc->lvl_start = q->lvl_start;
+  for (int d = 0; d < gqs::kLevels; ++d) {
+    for (int c = 0; c < 4; ++c) acc->lvl[d][c] += q->lvl[d][c];
+    if (!acc->lvl[d][4] || (q->lvl[d][4] && q->lvl[d][4] < acc->lvl[d][4])) acc->lvl[d][4] = q->lvl[d][4];
+    if (q->lvl[d][5] > acc->lvl[d][5]) acc->lvl[d][5] = q->lvl[d][5];
+  }
+#endif
 }
 
 // The host-pointer sort of a large array, overlapping the copies with the work: piece i is
@@ -800,6 +816,33 @@ int gqs_last_profile(gqs_ctx* c, uint64_t* out, size_t n) {
   const size_t k = n < 32 ? n : 32;
   for (size_t i = 0; i < k; ++i) out[i] = c->last_prof[i];
   return (int)k;
+}
+
+int gqs_last_levels(gqs_ctx* c, gqs_level* out, int max) {
+  if (!c || !out || max <= 0) return 0;
+  std::lock_guard<std::mutex> lk(c->mu);
+  DeviceGuard dg(c->device);
+  (void)wait_pending_locked(c);
+#ifdef GQS_PROFILE
+  int k = 0;
+  for (int d = 0; d < gqs::kLevels && k < max; ++d) {
+    const unsigned long long* r = c->last_lvl[d];
+    if (!r[0] && !r[2]) continue;
+    gqs_level& L = out[k++];
+    L.depth = (uint32_t)d;
+    L.part_jobs = (uint32_t)r[0];
+    L.part_keys = r[1];
+    L.local_jobs = (uint32_t)r[2];
+    L.reserved = 0;
+    L.local_keys = r[3];
+    const long long t0 = (long long)c->last_lvl_start;
+    L.first_ms = r[4] ? (double)((long long)r[4] - t0) / 1e6 : 0.0;
+    L.last_ms = r[5] ? (double)((long long)r[5] - t0) / 1e6 : 0.0;
+  }
+  return k;
+#else
+  return 0;
+#endif
 }
 
 int gqs_variant_count(int dtype) { return gqs::variant_count(dtype); }

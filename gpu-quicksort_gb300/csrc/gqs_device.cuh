@@ -52,6 +52,8 @@ static_assert(sizeof(Job) == 80, "job record layout");
 // Work is handed out by ticket: `grab` counts tickets taken, the low half of `alloc` counts
 // tickets created and its high half job records created. The ticket map (SortArgs::tmap)
 // holds ((ticket + 1) << 32 | job slot) at index ticket & tmask once the job is published.
+constexpr int kLevels = 48;  // rows of the per-level statistics of a -DGQS_PROFILE build
+
 struct Queue {
   unsigned long long total;  // keys in this sort
   unsigned long long done;   // keys in their final place
@@ -61,6 +63,14 @@ struct Queue {
   unsigned long long part_keys, local_keys, tiny_keys, fill_keys, chunks;
   uint32_t part_jobs, local_jobs, fill_jobs, max_depth;
   unsigned long long prof[32];  // cycle counters of a -DGQS_PROFILE build (zero otherwise)
+#ifdef GQS_PROFILE
+  // Per partition level (job depth; the last row takes every deeper level) in a -DGQS_PROFILE
+  // build, the counterpart of the reference's optional per-level timing: partition jobs and
+  // their keys, on-chip jobs and their keys, and the global-timer times of a first and the
+  // last completion at that depth; lvl_start is the first CTA's start.
+  unsigned long long lvl_start;
+  unsigned long long lvl[kLevels][6];
+#endif
 };
 
 // Optional cycle accounting per role (compile with -DGQS_PROFILE); slots:
@@ -251,6 +261,19 @@ struct alignas(128) Smem {
 __device__ __forceinline__ void set_error(Queue* q, uint32_t code, unsigned long long info) {
   if (atomicCAS(&q->error, 0u, code) == 0u) q->error_info = info;
 }
+
+#ifdef GQS_PROFILE
+// Counts one finished job of `keys` keys at `depth` in the per-level rows (col 0: partition
+// jobs, col 2: on-chip sorts) and notes the time. One thread per job.
+__device__ __forceinline__ void level_note(Queue* q, uint32_t depth, int col, unsigned long long keys) {
+  unsigned long long* r = q->lvl[depth < (uint32_t)kLevels ? depth : (uint32_t)kLevels - 1u];
+  atomicAdd(&r[col], 1ull);
+  atomicAdd(&r[col + 1], keys);
+  const unsigned long long now = global_timer_ns();
+  atomicCAS(&r[4], 0ull, now);
+  atomicMax(&r[5], now);
+}
+#endif
 
 // Debug builds (-DGQS_CHECK) test every job record, staged range and global write index
 // against the sort's bounds; a failed test records ST_BOUNDS with the site's code in
@@ -889,6 +912,9 @@ struct Persistent {
     const B pv = (B)__ldcg(&j->pivot);
     const uint32_t dir = __ldcg(&j->dir), depth = __ldcg(&j->depth);
     if (!GQS_OK(js <= ss && ss <= se && se <= je && je <= a.n, a.q, 0xB00Aull)) return;
+#ifdef GQS_PROFILE
+    if (lane == 0) level_note(a.q, depth, 0, je - js);
+#endif
     unsigned long long placed = 0;
     // Pivot run [ss, se) -> d (the reference's last block writes it serially,
     // QuicksortKernels.cl:214-216; here a warp writes short runs and long runs become
@@ -1712,6 +1738,9 @@ struct Persistent {
         if (tid == 0) {
           mbar_arrive(&sm.lempty);
           atomicAdd(&a.q->done, (unsigned long long)m);
+#ifdef GQS_PROFILE
+          level_note(a.q, __ldcg(&a.jobs[dd.job].depth), 2, m);
+#endif
         }
         GQS_PROF_ADD(PF_C_LSTORE, ts)
         st_local += m;
@@ -1764,6 +1793,9 @@ __global__ void __launch_bounds__(C::NT, min_blocks_per_sm<C>()) persistent_kern
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
+#ifdef GQS_PROFILE
+  if (tid == 0) atomicCAS(&a.q->lvl_start, 0ull, (unsigned long long)global_timer_ns());
+#endif
   const int warp = tid >> 5;
   if (warp < C::NCW) {
     Persistent<C>::consumers(a, sm);

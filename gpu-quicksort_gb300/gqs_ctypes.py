@@ -31,7 +31,7 @@ EXPORTS = [
     "gqs_sort_u32_dev", "gqs_sort_f32_dev", "gqs_sort_f64_dev",
     "gqs_sort_segments_u32_dev", "gqs_sort_segments_f32_dev", "gqs_sort_segments_f64_dev",
     "gqs_sort_segments_u32", "gqs_sort_segments_f32", "gqs_sort_segments_f64",
-    "gqs_sort_u32_noalloc", "gqs_sync", "gqs_last_stats", "gqs_last_profile", "gqs_variant_count", "gqs_variant_describe", "gqs_set_variant",
+    "gqs_sort_u32_noalloc", "gqs_sync", "gqs_last_stats", "gqs_last_profile", "gqs_last_levels", "gqs_variant_count", "gqs_variant_describe", "gqs_set_variant",
     "gqs_get_variant", "gqs_strerror", "gqs_version",
     "gqs_batch_create", "gqs_batch_destroy", "gqs_batch_keys", "gqs_batch_offsets", "gqs_batch_launch",
     "gqs_batch_wait", "gqs_batch_copy_in", "gqs_batch_copy_out", "gqs_batch_set_variant", "gqs_batch_get_variant", "gqs_batch_autotune",
@@ -64,6 +64,12 @@ class Stats(C.Structure):
 
     def as_dict(self) -> dict:
         return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+class Level(C.Structure):
+    _fields_ = [("depth", C.c_uint32), ("part_jobs", C.c_uint32), ("part_keys", C.c_uint64),
+                ("local_jobs", C.c_uint32), ("reserved", C.c_uint32), ("local_keys", C.c_uint64),
+                ("first_ms", C.c_double), ("last_ms", C.c_double)]
 
 
 class VariantDesc(C.Structure):
@@ -146,6 +152,8 @@ def load_library(path: str | None = None) -> C.CDLL:
     lib.gqs_last_stats.restype = st
     lib.gqs_last_profile.argtypes = [vp, C.POINTER(C.c_uint64), sz]
     lib.gqs_last_profile.restype = C.c_int
+    lib.gqs_last_levels.argtypes = [vp, C.POINTER(Level), C.c_int]
+    lib.gqs_last_levels.restype = C.c_int
     lib.gqs_variant_count.argtypes = [C.c_int]
     lib.gqs_variant_count.restype = C.c_int
     lib.gqs_variant_describe.argtypes = [C.c_int, C.c_int, C.POINTER(VariantDesc)]
@@ -317,6 +325,12 @@ class Context:
 
     def set_variant(self, dtype: str, v: int) -> None:
         _check(self.lib.gqs_set_variant(self.h, DTYPES[dtype], v), "gqs_set_variant")
+
+    def levels(self) -> list[dict]:
+        """Per-level rows of the last sort (profiling library only; [] otherwise)."""
+        buf = (Level * 64)()
+        k = self.lib.gqs_last_levels(self.h, buf, 64)
+        return [{f: getattr(buf[i], f) for f, _ in Level._fields_ if f != "reserved"} for i in range(k)]
 
     def selftest_bounds(self, dtype: str) -> int:
         """Sorts keys under a deliberately short index bound; a -DGQS_CHECK build reports

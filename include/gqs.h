@@ -287,6 +287,25 @@ gqs_status gqs_last_stats(gqs_ctx* ctx, gqs_stats* out);
  * (zeros otherwise). Writes up to n values and returns the number written. */
 int gqs_last_profile(gqs_ctx* ctx, uint64_t* out, size_t n);
 
+/* One partition level (job depth; the root job is depth 0) of the last sort. */
+typedef struct gqs_level {
+  uint32_t depth;
+  uint32_t part_jobs;  /* partition jobs that finished at this depth */
+  uint64_t part_keys;  /* the keys they partitioned */
+  uint32_t local_jobs; /* on-chip sorts of ranges at this depth */
+  uint32_t reserved;
+  uint64_t local_keys; /* the keys they sorted */
+  double first_ms;     /* a first and the last job completion at this depth, ms after the */
+  double last_ms;      /* persistent kernel started */
+} gqs_level;
+
+/* Per-level statistics of the context's last sort, the counterpart of the reference's optional
+ * per-level timing (GET_DETAILED_PERFORMANCE, GPU-Quicksort_OpenCL_1.2/QuicksortMain.cpp:148,
+ * 226-252): fills up to `max` rows, one per depth with any work (depths beyond 47 share the
+ * last row), and returns how many. Only the profiling flavour of the library
+ * (libgqs_prof.so) records them; the product library returns 0. */
+int gqs_last_levels(gqs_ctx* ctx, gqs_level* out, int max);
+
 /* Kernel variants available for a key type, and the one the context currently uses. */
 int gqs_variant_count(int dtype);
 gqs_status gqs_variant_describe(int dtype, int variant, gqs_variant_desc* out);
