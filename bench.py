@@ -55,8 +55,10 @@ def parse():
     p.add_argument("--profile", action="store_true", help="use libgqs_prof.so and print its cycle counters")
     p.add_argument("--serve-requests", type=int, default=20000,
                    help="requests of the serving stream (--config serve, and the summary in the plain line; 0: skip)")
-    p.add_argument("--serve-load", type=float, default=0.7,
-                   help="Poisson offered load as a fraction of the batched server's measured capacity")
+    p.add_argument("--serve-load", type=float, default=0.5,
+                   help="Poisson offered load as a fraction of each server's measured saturation capacity "
+                        "(Poisson arrivals form smaller batches than saturation, so the batched server's "
+                        "capacity under them is lower: 0.7 sits at its edge)")
     return p.parse_args()
 
 
