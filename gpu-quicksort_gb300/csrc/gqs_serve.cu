@@ -39,6 +39,7 @@
 #include <vector>
 
 #include "gqs.h"
+#include "gqs_arena.h"
 #include "gqs_graph.h"
 #include "gqs_host.h"
 
@@ -50,52 +51,7 @@ uint64_t now_ns() {
       .count();
 }
 
-constexpr size_t kGrain = 256;  // arena allocation granularity (bytes)
-
-// First-fit allocator over [0, size) with coalescing frees.
-class ArenaAlloc {
- public:
-  void reset(size_t size) {
-    free_.clear();
-    if (size) free_[0] = size;
-    used_ = 0;
-  }
-  bool alloc(size_t bytes, size_t* off) {
-    bytes = (bytes + kGrain - 1) / kGrain * kGrain;
-    for (auto it = free_.begin(); it != free_.end(); ++it) {
-      if (it->second < bytes) continue;
-      *off = it->first;
-      const size_t rest = it->second - bytes, at = it->first + bytes;
-      free_.erase(it);
-      if (rest) free_[at] = rest;
-      used_ += bytes;
-      return true;
-    }
-    return false;
-  }
-  void release(size_t off, size_t bytes) {
-    bytes = (bytes + kGrain - 1) / kGrain * kGrain;
-    used_ -= bytes;
-    auto next = free_.lower_bound(off);
-    if (next != free_.end() && off + bytes == next->first) {
-      bytes += next->second;
-      next = free_.erase(next);
-    }
-    if (next != free_.begin()) {
-      auto prev = std::prev(next);
-      if (prev->first + prev->second == off) {
-        prev->second += bytes;
-        return;
-      }
-    }
-    free_[off] = bytes;
-  }
-  size_t used() const { return used_; }
-
- private:
-  std::map<size_t, size_t> free_;
-  size_t used_ = 0;
-};
+using gqs::ArenaAlloc;
 
 struct Req {
   uint64_t id = 0;
@@ -520,11 +476,11 @@ gqs_status gqs_srv_create(int device, const gqs_server_config* cfg, gqs_server**
       if (st != GQS_OK) break;
       lane_bytes += 0;
     }
-    if (c.budget_bytes <= lane_bytes + 2 * kGrain) {
+    if (c.budget_bytes <= lane_bytes + 2 * gqs::kArenaGrain) {
       st = GQS_ERR_INVALID;
       break;
     }
-    s->arena_bytes = (c.budget_bytes - lane_bytes) / 2 / kGrain * kGrain;
+    s->arena_bytes = (c.budget_bytes - lane_bytes) / 2 / gqs::kArenaGrain * gqs::kArenaGrain;
     st = gqs::cuda_status(cudaMalloc(&s->keys, s->arena_bytes));
     if (st != GQS_OK) break;
     st = gqs::cuda_status(cudaMalloc(&s->scratch, s->arena_bytes));
@@ -559,7 +515,7 @@ gqs_status gqs_srv_submit(gqs_server* s, int dtype, const void* in, void* out, s
   const size_t es = gqs::kElemSize[dtype];
   if (n == 0 || n > s->cfg.batch_keys || !in || !out) return GQS_ERR_INVALID;
   if ((reinterpret_cast<uintptr_t>(in) % es) || (reinterpret_cast<uintptr_t>(out) % es)) return GQS_ERR_INVALID;
-  if ((n * es + kGrain - 1) / kGrain * kGrain > s->arena_bytes) return GQS_ERR_NOMEM;  // can never fit
+  if ((n * es + gqs::kArenaGrain - 1) / gqs::kArenaGrain * gqs::kArenaGrain > s->arena_bytes) return GQS_ERR_NOMEM;  // can never fit
   // Results go back asynchronously only into page-locked memory; pageable output is copied
   // back synchronously when the batch retires.
   bool out_pinned = false;
