@@ -19,6 +19,7 @@ Multi-GPU (torchrun): every rank sorts its own array (replicas; no collective on
 from __future__ import annotations
 
 import argparse
+import gc
 import json
 import os
 import platform
@@ -331,6 +332,10 @@ def run_serve_arm(gqs_ctypes, templates, stream, per_request, rate, pool, sample
             got += 1
 
     col = threading.Thread(target=collect)
+    # no garbage-collector pauses inside the measured stream (they would show as request
+    # latency of the Python load generator, not of the server)
+    gc.collect()
+    gc.disable()
     col.start()
     t0 = srv.now_ns()
     t_wall0 = time.perf_counter()
@@ -348,6 +353,7 @@ def run_serve_arm(gqs_ctypes, templates, stream, per_request, rate, pool, sample
             rid = srv.submit_raw(t, tmpl.data_ptr() + int(src[i]) * esz[dt[i]], pool.base + rec[0], int(n[i]))
             idx_of[rid] = i
     col.join()
+    gc.enable()
     st = srv.stats()
     srv.close()
     done = np.array([x["t_done_ns"] for x in info], dtype=np.float64)
