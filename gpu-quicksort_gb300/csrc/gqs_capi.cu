@@ -161,6 +161,15 @@ gqs_status wait_pending_locked(gqs_ctx* c) {
   return (gqs_status)s.status;
 }
 
+// Returns `st` after a failure once copies of a caller's host array are queued, when neither
+// stream can still read or write that array.
+gqs_status drain(gqs_ctx* c, gqs_status st) {
+  cudaStreamSynchronize(c->copy_stream);
+  cudaStreamSynchronize(c->stream);
+  (void)cudaGetLastError();
+  return st;
+}
+
 // Validates, grows pools, and enqueues one sort on `stream`. Caller holds the lock.
 gqs_status enqueue_locked(gqs_ctx* c, int dtype, void* d, void* dn, size_t n, const unsigned long long* offsets,
                           size_t nseg, cudaStream_t stream, unsigned long long check_n = 0) {
@@ -316,11 +325,11 @@ gqs_status sort_host_pipelined(gqs_ctx* c, int dtype, void* d, size_t n) {
     e = cudaMemcpyAsync(dd + off[i] * es, hd + off[i] * es, len * es, cudaMemcpyHostToDevice, c->copy_stream);
     if (e == cudaSuccess) e = cudaEventRecord(c->ev_piece[i], c->copy_stream);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(c->stream, c->ev_piece[i], 0);
-    if (e != cudaSuccess) return cuda_status(e);
+    if (e != cudaSuccess) return drain(c, cuda_status(e));
     gqs_status st = enqueue_locked(c, dtype, dd + off[i] * es, dn + off[i] * es, len, nullptr, 1, c->stream);
-    if (st != GQS_OK) return st;
+    if (st != GQS_OK) return drain(c, st);
     accumulate_queue<<<1, 1, 0, c->stream>>>(c->q, c->q_acc);
-    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_status(e);
+    if ((e = cudaGetLastError()) != cudaSuccess) return drain(c, cuda_status(e));
   }
   // pieces 0+1 and 2+3 into the scratch, then the two halves back into pool_d, in kSlices
   // launches: each slice of the result goes back to the host on the copy stream while the
@@ -344,7 +353,7 @@ gqs_status sort_host_pipelined(gqs_ctx* c, int dtype, void* d, size_t n) {
   }
   // the last copy follows every kernel of this call (it waited for the last slice)
   if (e == cudaSuccess) e = cudaEventRecord(c->ev_done, c->copy_stream);
-  if (e != cudaSuccess) return cuda_status(e);
+  if (e != cudaSuccess) return drain(c, cuda_status(e));
   c->pending_acc = true;
   c->pending_timed = false;
   return wait_pending_locked(c);
@@ -365,13 +374,13 @@ gqs_status sort_host(gqs_ctx* c, int dtype, void* d, size_t n) {
     if (st != GQS_OK) return st;
   }
   cudaError_t e = cudaMemcpyAsync(c->pool_d, d, bytes, cudaMemcpyHostToDevice, c->stream);
-  if (e != cudaSuccess) return cuda_status(e);
+  if (e != cudaSuccess) return drain(c, cuda_status(e));
   gqs_status st = enqueue_locked(c, dtype, c->pool_d, nullptr, n, nullptr, 1, c->stream);
-  if (st != GQS_OK) return st;
+  if (st != GQS_OK) return drain(c, st);
   e = cudaMemcpyAsync(d, c->pool_d, bytes, cudaMemcpyDeviceToHost, c->stream);
-  if (e != cudaSuccess) return cuda_status(e);
+  if (e != cudaSuccess) return drain(c, cuda_status(e));
   e = cudaEventRecord(c->ev_done, c->stream);
-  if (e != cudaSuccess) return cuda_status(e);
+  if (e != cudaSuccess) return drain(c, cuda_status(e));
   return wait_pending_locked(c);
 }
 
@@ -411,15 +420,15 @@ gqs_status sort_segments_host(gqs_ctx* c, int dtype, void* keys, size_t n, const
     if (st != GQS_OK) return st;
   }
   cudaError_t e = cudaMemcpyAsync(c->pool_d, keys, bytes, cudaMemcpyHostToDevice, c->stream);
-  if (e != cudaSuccess) return cuda_status(e);
+  if (e != cudaSuccess) return drain(c, cuda_status(e));
   e = cudaMemcpyAsync(c->offs, offsets, obytes, cudaMemcpyHostToDevice, c->stream);
-  if (e != cudaSuccess) return cuda_status(e);
+  if (e != cudaSuccess) return drain(c, cuda_status(e));
   gqs_status st = enqueue_locked(c, dtype, c->pool_d, nullptr, n, c->offs, nseg, c->stream);
-  if (st != GQS_OK) return st;
+  if (st != GQS_OK) return drain(c, st);
   e = cudaMemcpyAsync(keys, c->pool_d, bytes, cudaMemcpyDeviceToHost, c->stream);
-  if (e != cudaSuccess) return cuda_status(e);
+  if (e != cudaSuccess) return drain(c, cuda_status(e));
   e = cudaEventRecord(c->ev_done, c->stream);
-  if (e != cudaSuccess) return cuda_status(e);
+  if (e != cudaSuccess) return drain(c, cuda_status(e));
   return wait_pending_locked(c);
 }
 
@@ -510,13 +519,13 @@ gqs_status sort_pairs_host(gqs_ctx* c, bool is_float, uint32_t* keys, uint32_t* 
   uint32_t* dv = static_cast<uint32_t*>(c->pool_v);
   cudaError_t e = cudaMemcpyAsync(dk, keys, bytes, cudaMemcpyHostToDevice, c->stream);
   if (e == cudaSuccess) e = cudaMemcpyAsync(dv, vals, bytes, cudaMemcpyHostToDevice, c->stream);
-  if (e != cudaSuccess) return cuda_status(e);
+  if (e != cudaSuccess) return drain(c, cuda_status(e));
   gqs_status st = enqueue_pairs_locked(c, is_float, dk, dv, n, c->stream);
-  if (st != GQS_OK) return st;
+  if (st != GQS_OK) return drain(c, st);
   e = cudaMemcpyAsync(keys, dk, bytes, cudaMemcpyDeviceToHost, c->stream);
   if (e == cudaSuccess) e = cudaMemcpyAsync(vals, dv, bytes, cudaMemcpyDeviceToHost, c->stream);
   if (e == cudaSuccess) e = cudaEventRecord(c->ev_done, c->stream);
-  if (e != cudaSuccess) return cuda_status(e);
+  if (e != cudaSuccess) return drain(c, cuda_status(e));
   return wait_pending_locked(c);
 }
 
