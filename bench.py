@@ -12,19 +12,30 @@ uniformly over [0, 2^32) from a fixed seed. A step is one sort of that array.
             chunks + keys sorted on chip + keys sorted in registers, from the kernel's own
             counters) / its CUDA-event duration, against the measured HBM copy bandwidth
 
+  configs   every other configuration of the benchmark, each with its own kernel time, roofline
+            fraction, clock record and a bit-exact check against the std::sort digest committed in
+            tests/golden/full_size.json: 2^20 u32; 2^28 u32 sorted / reverse / 16 distinct /
+            Zipf(1.1) / Gaussian; 2^27 f32 N(0, 1e3); 2^26 f64 U[-1e9, 1e9]; the batched sort of
+            4096 arrays (autotuned variant, against one plain call per array, end to end)
+  phases    the split of the 2^28 kernel's time between partition chunks and on-chip sorts
+
 Options: --impl reference times the reference's CPU path (the oracle's restatement of
-GPUQSort<T>, all host threads) on a bounded sample; --config batched runs the segmented form.
+GPUQSort<T>, all host threads) on the same 2^28 array, beside std::sort on one core and the
+parallel std::sort on all cores; --config batched runs the segmented form alone.
 Multi-GPU (torchrun): every rank sorts its own array (replicas; no collective on the data path).
 """
 from __future__ import annotations
 
 import argparse
 import gc
+import hashlib
 import json
+import math
 import os
 import platform
 import subprocess
 import sys
+import threading
 import time
 
 import numpy as np
@@ -53,6 +64,7 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-clocks", action="store_true")
+    p.add_argument("--no-configs", action="store_true", help="skip the list of the other configurations")
     p.add_argument("--profile", action="store_true", help="use libgqs_prof.so and print its cycle counters")
     p.add_argument("--serve-requests", type=int, default=20000,
                    help="requests of the serving stream (--config serve, and the summary in the plain line; 0: skip)")
@@ -81,8 +93,8 @@ def max_over_ranks(x, dist):
     return float(t.item())
 
 
-def workload_name(args, n):
-    if args.config == "batched":
+def workload_name(args, n, batched=False):
+    if batched or args.config == "batched":
         return f"batched segmented sort: 4096 uint32 arrays, lengths log-uniform in [32, 2^20], {n} keys"
     if args.config == "tiles":
         return f"segmented sort of 8000-key {args.dtype} arrays (on-chip sort only), {n} keys"
@@ -110,51 +122,114 @@ def ncu_traffic(workload_key):
 
 
 class ClockSampler:
+    """nvidia-smi samples (every 50 ms) of the SM clock and the throttle reasons, read by a thread
+    as they arrive and stamped with the host's monotonic clock, so that each timed region can be
+    given the samples taken during it."""
+
+    REASONS = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+
     def __init__(self, enabled, index=0):
         self.proc = None
-        self.path = None
+        self.samples = []  # (t, sm_mhz, sm_max_mhz, reasons)
+        self.lock = threading.Lock()
         if not enabled:
             return
         q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
-        os.makedirs(os.path.join(ROOT, "gpurun_out"), exist_ok=True)
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_bench_{os.getpid()}.csv")
         try:
-            self.f = open(self.path, "w")
-            self.proc = subprocess.Popen(["nvidia-smi", f"--id={index}", f"--query-gpu={q}", "--format=csv,noheader,nounits",
-                                          "-lms", "50"], stdout=self.f, stderr=subprocess.DEVNULL)
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={index}", f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True, bufsize=1)
         except Exception:
             self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
 
-    def stop(self):
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm, mx = float(parts[1]), float(parts[2])
+            except ValueError:
+                continue
+            reasons = {nm for nm, v in zip(self.REASONS, parts[5:9]) if v.lower() == "active"}
+            with self.lock:
+                self.samples.append((time.perf_counter(), sm, mx, reasons))
+
+    def ready(self, timeout=5.0):
+        """Waits until the first sample has arrived (the sampler takes a moment to start)."""
+        t_end = time.perf_counter() + timeout
+        while self.proc and time.perf_counter() < t_end:
+            with self.lock:
+                if self.samples:
+                    return True
+            time.sleep(0.02)
+        return False
+
+    def window(self, t0=None, t1=None):
+        """Summary of the samples taken in [t0, t1] (all samples without bounds); a region shorter
+        than the sampling interval gets the nearest sample on each side."""
         if not self.proc:
             return None
-        self.proc.terminate()
-        try:
-            self.proc.wait(timeout=5)
-        except Exception:
-            self.proc.kill()
-        self.f.close()
-        sm, mx, reasons = [], [], set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        with open(self.path) as f:
-            for line in f:
-                parts = [x.strip() for x in line.split(",")]
-                if len(parts) < 9:
-                    continue
-                try:
-                    sm.append(float(parts[1]))
-                    mx.append(float(parts[2]))
-                except ValueError:
-                    continue
-                for nm, v in zip(names, parts[5:9]):
-                    if v.lower() == "active":
-                        reasons.add(nm)
-        if not sm:
+        time.sleep(0.06)  # let the sample that closes the region arrive
+        with self.lock:
+            smp = list(self.samples)
+        if not smp:
             return None
-        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
-                "samples": len(sm)}
+        if t0 is not None:
+            inside = [x for x in smp if t0 <= x[0] <= t1]
+            if not inside:
+                before = [x for x in smp if x[0] < t0][-1:]
+                after = [x for x in smp if x[0] > t1][:1]
+                inside = before + after
+            smp = inside or smp[-1:]
+        sm = [x[1] for x in smp]
+        reasons = set().union(*[x[3] for x in smp])
+        return {"sm_mhz": float(np.median(sm)), "sm_min_mhz": float(min(sm)),
+                "sm_max_mhz": float(max(x[2] for x in smp)), "reasons": sorted(reasons), "samples": len(smp)}
+
+    def stop(self):
+        summary = self.window()
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.proc = None
+        return summary
+
+
+# ---------------------------------------------------------------------------
+# Bit-exact checks against the committed std::sort digests of every configuration
+
+def sha256_of(a) -> str:
+    return hashlib.sha256(memoryview(np.ascontiguousarray(a)).cast("B")).hexdigest()
+
+
+def golden_case(dtype, dist, n, seed, kind="plain"):
+    """The std::sort digest of one configuration (tests/golden/full_size.json), or None."""
+    try:
+        with open(os.path.join(ROOT, "tests", "golden", "full_size.json")) as f:
+            cases = json.load(f)["cases"]
+    except Exception:
+        return None
+    for c in cases:
+        if c["kind"] == kind and c["dtype"] == dtype and c["dist"] == dist and c["n"] == n and c["seed"] == seed:
+            return c
+    return None
+
+
+def golden_check(case, host_in, host_out):
+    """Compares the seeded input and the GPU's output (host arrays) with the golden digests."""
+    if case is None:
+        return {"golden": "no committed digest for this input"}
+    return {"input_sha256_equal_to_golden": sha256_of(host_in) == case["input_sha256"],
+            "bit_exact_vs_std_sort_digest": sha256_of(host_out) == case["sorted_sha256"]}
 
 
 def cpu_baseline(args, n_full):
@@ -199,6 +274,10 @@ def cpu_baseline(args, n_full):
 
 
 def run_reference(args):
+    """The reference's CPU path on the benchmark's own array (2^log2n keys, not a sample): the
+    oracle's restatement of GPUQSort<T> on all host threads, `warmup` + `steps` sorts; beside it,
+    once each on the same array, std::sort on one core (the reference's verifier) and GCC's
+    parallel sort on all cores (for the reference's tbb::parallel_sort)."""
     rank, world, _ = dist_env()
     if rank != 0:
         return
@@ -206,27 +285,43 @@ def run_reference(args):
     import gqs_ctypes
     import oracle_ctypes
     threads = os.cpu_count() or 1
-    n_full = 1 << args.log2n
-    ns = min(n_full, 1 << 24)
-    a = gqs_ctypes.generate(args.dtype, args.dist, SEED, ns)
+    n = 1 << args.log2n
+    a = gqs_ctypes.generate(args.dtype, args.dist, SEED, n)
+    b = np.empty_like(a)
     for _ in range(args.warmup):
-        b = a.copy()
+        np.copyto(b, a)
         oracle_ctypes.gpuqsort(b, threads=threads)
     times = []
     for _ in range(args.steps):
-        b = a.copy()
+        np.copyto(b, a)
         t0 = time.perf_counter()
         oracle_ctypes.gpuqsort(b, threads=threads)
         times.append(time.perf_counter() - t0)
-    v = ns * len(times) / sum(times) / 1e9
+    v = n * len(times) / sum(times) / 1e9
+    np.copyto(b, a)
+    t0 = time.perf_counter()
+    oracle_ctypes.std_sort(b)
+    t_std = time.perf_counter() - t0
+    c = a.copy()
+    t0 = time.perf_counter()
+    oracle_ctypes.parallel_sort(c, threads)
+    t_par = time.perf_counter() - t0
+    same = bool(np.array_equal(b, c))
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "Gkeys/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": args.dtype,
             "data": "synthetic (seeded generator, gpu-quicksort_gb300/workload)",
-            "config": {"workload": workload_name(args, n_full), "sample_keys": ns},
+            "config": {"workload": workload_name(args, n), "keys": n, "seed": SEED},
             "cpu_baseline": {"value": v, "unit": "Gkeys/s", "cores": threads, "kind": "port",
-                             "sample": f"{ns} keys per step (bounded sample of the 2^{args.log2n} workload), "
-                                       "oracle restatement of GPUQSort<T>, all host threads"},
+                             "sample": f"the whole {n}-key array every step (no sample): the oracle's restatement "
+                                       "of GPUQSort<T> (oracle/gqs_oracle.cpp), all host threads",
+                             "std_sort_1core": {"value": n / t_std / 1e9, "unit": "Gkeys/s", "keys": n,
+                                                "s": t_std},
+                             "parallel_sort_all_cores": {"value": n / t_par / 1e9, "unit": "Gkeys/s", "keys": n,
+                                                         "threads": threads, "s": t_par,
+                                                         "what": "__gnu_parallel::sort, for tbb::parallel_sort"},
+                             "std_sort_equal_to_parallel_sort": same,
+                             "cpu": platform.processor() or platform.machine()},
             "e2e": {"value": v, "unit": "Gkeys/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -358,10 +453,26 @@ def run_serve_arm(gqs_ctypes, templates, stream, per_request, rate, pool, sample
     srv.close()
     done = np.array([x["t_done_ns"] for x in info], dtype=np.float64)
     sub = np.array([x["t_submit_ns"] for x in info], dtype=np.float64)
+    adm = np.array([x["t_admit_ns"] for x in info], dtype=np.float64)
+    lau = np.array([x["t_launch_ns"] for x in info], dtype=np.float64)
     arr_ns = t0 + arrive * 1e9 if rate else sub
     lat_ms = (done - np.minimum(arr_ns, sub)) / 1e6
     span = (done.max() - min(t0, sub.min())) / 1e9
-    return {"keys_per_s": float(n.sum()) / span, "span_s": span, "lat_ms": lat_ms,
+    # where the latency goes, per key type: arrival -> submit (the load generator's own lag),
+    # submit -> admit (waiting for arena memory), admit -> launch (resident, waiting for a lane
+    # and for its type's turn), launch -> done (its batch's sort and copy back)
+    split = {}
+    for k, t in enumerate(SERVE_TYPES):
+        m = dt == k
+        if not m.any():
+            continue
+        parts = {"arrive_submit": (sub[m] - np.minimum(arr_ns[m], sub[m])) / 1e6, "submit_admit": (adm[m] - sub[m]) / 1e6,
+                 "admit_launch": (lau[m] - adm[m]) / 1e6, "launch_done": (done[m] - lau[m]) / 1e6,
+                 "total": lat_ms[m]}
+        split[t] = {name: {"p50_ms": float(np.percentile(v, 50)), "p99_ms": float(np.percentile(v, 99))}
+                    for name, v in parts.items()}
+        split[t]["requests"] = int(m.sum())
+    return {"keys_per_s": float(n.sum()) / span, "span_s": span, "lat_ms": lat_ms, "split": split,
             "batches": st["batches"], "max_batch_requests": st["max_batch_requests"],
             "arena_peak_gb": st["arena_peak"] / 1e9}, samples
 
@@ -405,7 +516,8 @@ def run_serve(args, gqs_ctypes):
 
     def lat(r):
         return {"p50_ms": float(np.percentile(r["lat_ms"], 50)), "p99_ms": float(np.percentile(r["lat_ms"], 99)),
-                "gkeys_s": r["keys_per_s"] / 1e9, "span_s": r["span_s"], "batches": r["batches"]}
+                "gkeys_s": r["keys_per_s"] / 1e9, "span_s": r["span_s"], "batches": r["batches"],
+                "split_by_type": r["split"]}
 
     total_keys = int(n.sum())
     in_bytes = int(sum(int(n[i]) * (8 if dt[i] == 2 else 4) for i in range(count)))
@@ -488,9 +600,13 @@ def run_pairs(args, gqs_ctypes, rank, local, world, dist, barrier):
             "check": check, "gpu_launches": 4 * args.steps}
 
 
-def run_batched(args, gqs_ctypes, rank, local, world, dist, barrier):
-    """4096 uint32 arrays, lengths log-uniform in [32, 2^20], as one graph-captured batch."""
+def run_batched(args, gqs_ctypes, rank, local, world, dist, barrier, clocks=None, steps=None, warmup=None):
+    """4096 uint32 arrays, lengths log-uniform in [32, 2^20], as one graph-captured batch: the
+    autotuned variant's replays (value, roofline), the same arrays by one plain call each, and
+    the batch end to end through its host copy calls."""
     import torch
+    steps = steps or args.steps
+    warmup = warmup or args.warmup
     nseg = 4096
     off = gqs_ctypes.segment_offsets(SEED + rank, nseg, 32, 1 << 20)
     n = int(off[-1])
@@ -509,32 +625,49 @@ def run_batched(args, gqs_ctypes, rank, local, world, dist, barrier):
         tune = {"chosen": gqs_ctypes.variants("u32")[best]["name"],
                 "median_ms": {gqs_ctypes.variants("u32")[v]["name"]: m for v, m in enumerate(ms)}}
     stream = torch.cuda.current_stream()
-    clocks = ClockSampler(enabled=(not args.no_clocks and rank == 0), index=local)
+    own_clocks = clocks is None
+    if own_clocks:
+        clocks = ClockSampler(enabled=(not args.no_clocks and rank == 0), index=local)
+        clocks.ready()
 
     def step():
         rc = batch.launch(nseg, stream.cuda_stream)
         if rc != 0:
             raise RuntimeError(f"batch launch failed: {gqs_ctypes.STATUS.get(rc, rc)}")
 
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         arena.copy_(pristine)
         step()
         code, st = batch.wait()
         if code != 0:
             raise RuntimeError(f"batch failed: {st}")
-    # correctness: (segment, key) pairs sorted lexicographically equal the batch's output
+    # bit-exact checks of the last warm-up result: the std::sort digest of the whole output and of
+    # every segment, and (segment, key) pairs sorted lexicographically by torch
+    out_h = torch.empty_like(host_in, pin_memory=True)
+    ov = out_h.numpy().view(np.uint32)
+    out_h.copy_(arena)
+    case = golden_case("u32", "uniform", n, SEED + rank, kind="segments")
+    check = golden_check(case, hv, ov)
+    if case is not None:
+        bad = [i for i in range(nseg)
+               if hashlib.sha256(memoryview(ov[int(off[i]):int(off[i + 1])]).cast("B")).hexdigest()[:16]
+               != case["segment_sha256_16"][i]]
+        check["segments_equal_to_std_sort_digest"] = nseg - len(bad)
+        check["first_bad_segment"] = bad[0] if bad else None
     seg_id = torch.repeat_interleave(torch.arange(nseg, device="cuda", dtype=torch.int64),
                                      torch.from_numpy(np.diff(off).astype(np.int64)).cuda())
     keyed = (seg_id << 32) | (pristine.to(torch.int64) & 0xFFFFFFFF)
     ref = torch.sort(keyed).values & 0xFFFFFFFF
-    check = {"bit_exact_vs_torch_sort_per_segment": bool(torch.equal(arena.to(torch.int64) & 0xFFFFFFFF, ref))}
+    check["bit_exact_vs_torch_sort_per_segment"] = bool(torch.equal(arena.to(torch.int64) & 0xFFFFFFFF, ref))
     del seg_id, keyed, ref
-    ev0 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ev1 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    torch.cuda.empty_cache()
+    ev0 = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    ev1 = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
     kms, abytes = [], []
     barrier()
     torch.cuda.synchronize()
-    for i in range(args.steps):
+    t_0 = time.perf_counter()
+    for i in range(steps):
         arena.copy_(pristine)
         ev0[i].record(stream)
         step()
@@ -546,14 +679,15 @@ def run_batched(args, gqs_ctypes, rank, local, world, dist, barrier):
         abytes.append(st["algo_bytes"])
     torch.cuda.synchronize()
     barrier()
-    clk = clocks.stop()
+    t_1 = time.perf_counter()
+    clk = clocks.window(t_0, t_1)
+    if own_clocks:
+        clocks.stop()
     t = max_over_ranks(sum(a.elapsed_time(b) for a, b in zip(ev0, ev1)) / 1e3, dist)
-    value = n * world * args.steps / t / 1e9
+    value = n * world * steps / t / 1e9
     # end to end through the public batch calls: pinned host -> arena, replay, arena -> host
-    out = torch.empty_like(host_in, pin_memory=True)
-    ov = out.numpy().view(np.uint32)
     times = []
-    for i in range(args.steps + 1):
+    for i in range(steps + 1):
         t0 = time.perf_counter()
         batch.copy_in(hv)
         step()
@@ -562,9 +696,10 @@ def run_batched(args, gqs_ctypes, rank, local, world, dist, barrier):
         if i:
             times.append(time.perf_counter() - t0)
     tsum = max_over_ranks(sum(times), dist)
-    e2e = {"value": n * world * args.steps / tsum / 1e9, "unit": "Gkeys/s", "h2d_bytes_per_step": n * esize,
-           "d2h_bytes_per_step": n * esize, "ms_per_step": 1e3 * tsum / args.steps,
-           "api": "gqs_batch_copy_in + gqs_batch_launch + gqs_batch_wait + gqs_batch_copy_out (pinned)"}
+    e2e = {"value": n * world * steps / tsum / 1e9, "unit": "Gkeys/s", "h2d_bytes_per_step": n * esize,
+           "d2h_bytes_per_step": n * esize, "ms_per_step": 1e3 * tsum / steps,
+           "api": "gqs_batch_copy_in + gqs_batch_launch + gqs_batch_wait + gqs_batch_copy_out (pinned)",
+           "check": golden_check(case, hv, ov)}
     # the same arrays sorted by one plain call each (device pointers, enqueued back to back)
     ctx = gqs_ctypes.Context(device=local, sync=False, timing=False, variant=0)
     d = pristine.clone()
@@ -582,28 +717,253 @@ def run_batched(args, gqs_ctypes, rank, local, world, dist, barrier):
     plain_ms = e0.elapsed_time(e1)
     plain_same = bool(torch.equal(d, arena))
     ctx.close()
+    chosen = gqs_ctypes.variants("u32")[batch.variant]["name"]
+    batch.close()
+    del d, dn, arena, pristine
+    torch.cuda.empty_cache()
     if rank != 0:
         return None
     peak, peak_src = measured_peak()
     km, ab = float(np.mean(kms)), float(np.mean(abytes))
     achieved = ab / (km / 1e3) / 1e9
     return {
-        "metric": f"Gkeys/s ({workload_name(args, n)})", "value": value, "unit": "Gkeys/s", "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps, "higher_is_better": True,
+        "metric": f"Gkeys/s ({workload_name(args, n, batched=True)})", "workload": workload_name(args, n, batched=True),
+        "value": value, "unit": "Gkeys/s", "n_gpus": world,
+        "steps": steps, "warmup": warmup, "ms_per_step": 1e3 * t / steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u32",
         "data": "synthetic (seeded generator, gpu-quicksort_gb300/workload)",
-        "config": {"workload": workload_name(args, n), "keys": n, "segments": nseg, "seed": SEED,
+        "config": {"workload": workload_name(args, n, batched=True), "keys": n, "segments": nseg, "seed": SEED,
                    "l2": "inputs larger than L2 (arena rewritten from a pristine copy before every step)",
-                   "variant": gqs_ctypes.variants("u32")[batch.variant]["name"], "graph": "one cudaGraphLaunch per step",
-                   "parallelism": f"replicas x{world}"},
+                   "variant": chosen,
+                   "graph": "one cudaGraphLaunch per step", "parallelism": f"replicas x{world}"},
         "autotune": tune,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": ncu_traffic("batched_u32"), "kernel": "gqs::persistent_kernel (graph replay)",
                      "kernel_ms": km, "algo_bytes_per_launch": ab, "peak_source": peak_src},
+        "kernel_ms": km,
         "plain_per_array": {"gkeys_s": n / (plain_ms / 1e3) / 1e9, "ms": plain_ms, "calls": nseg,
-                            "same_output": plain_same},
-        "cpu_baseline": None, "e2e": e2e, "gpu_launches": 2 * args.steps, "clocks": clk, "check": check,
+                            "same_output": plain_same, "batched_speedup": value / (n / (plain_ms / 1e3) / 1e9)},
+        "cpu_baseline": None, "e2e": e2e, "gpu_launches": 2 * steps, "clocks": clk, "check": check,
     }
+
+
+def run_tiles(args, gqs_ctypes, rank, local, world, dist, barrier, peak, peak_src):
+    """The on-chip sort alone: a segmented sort of 8000-key arrays (6000 for f64), every array
+    one tile, so the kernel does no partition chunk."""
+    import torch
+    npdt = gqs_ctypes.NP_DTYPES[args.dtype]
+    esize = np.dtype(npdt).itemsize
+    seg = 6000 if args.dtype == "f64" else 8000
+    nseg = (1 << args.log2n) // seg
+    off = np.arange(nseg + 1, dtype=np.int64) * seg
+    n = int(off[-1])
+    offsets = torch.from_numpy(off).cuda()
+    host_in = torch.empty(n * esize, dtype=torch.uint8, pin_memory=True)
+    hv = host_in.numpy().view(npdt)
+    gqs_ctypes.generate(args.dtype, args.dist, SEED + rank, n, out=hv)
+    pristine = host_in.cuda()
+    d, dn = torch.empty_like(pristine), torch.empty_like(pristine)
+    ctx = gqs_ctypes.Context(device=local, sync=False, timing=True, variant=args.variant)
+    stream = torch.cuda.current_stream()
+    clocks = ClockSampler(enabled=(not args.no_clocks and rank == 0), index=local)
+    clocks.ready()
+
+    def sort_once():
+        rc = ctx.sort_segments_dev(args.dtype, d.data_ptr(), dn.data_ptr(), n, offsets.data_ptr(), nseg,
+                                   stream.cuda_stream)
+        if rc != 0:
+            raise RuntimeError(f"sort enqueue failed: {gqs_ctypes.STATUS.get(rc, rc)}")
+
+    for _ in range(args.warmup):
+        d.copy_(pristine)
+        sort_once()
+        if ctx.stats()["status"] != 0:
+            raise RuntimeError("sort failed")
+    out = d.cpu().numpy().view(npdt)
+    ok = all(np.array_equal(out[int(off[i]):int(off[i + 1])], np.sort(hv[int(off[i]):int(off[i + 1])]))
+             for i in range(0, nseg, max(1, nseg // 64)))
+    kms, abytes, step_ms = [], [], []
+    barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        d.copy_(pristine)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        sort_once()
+        e1.record(stream)
+        st = ctx.stats()
+        if st["status"] != 0:
+            raise RuntimeError("sort failed")
+        kms.append(st["kernel_ms"])
+        abytes.append(st["algo_bytes"])
+        step_ms.append(e0.elapsed_time(e1))
+    torch.cuda.synchronize()
+    barrier()
+    clk = clocks.window(t0, time.perf_counter())
+    clocks.stop()
+    phases = ctx.phases()
+    ctx.close()
+    t = max_over_ranks(sum(step_ms) / 1e3, dist)
+    km, ab = float(np.mean(kms)), float(np.mean(abytes))
+    return {"metric": f"Gkeys/s ({workload_name(args, n)})", "value": n * world * args.steps / t / 1e9,
+            "unit": "Gkeys/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * t / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": args.dtype, "data": "synthetic (seeded generator, gpu-quicksort_gb300/workload)",
+            "config": {"workload": workload_name(args, n), "keys": n, "segments": nseg, "segment_keys": seg,
+                       "variant": gqs_ctypes.variants(args.dtype)[st["variant"]]["name"]},
+            "roofline": {"bound": "hbm", "achieved": ab / (km / 1e3) / 1e9, "peak": peak, "unit": "GB/s",
+                         "frac": ab / (km / 1e3) / 1e9 / peak, "kernel_ms": km, "algo_bytes_per_launch": ab,
+                         "peak_source": peak_src},
+            "kernel_gkeys_s": n / (km / 1e3) / 1e9, "phases": phases, "clocks": clk,
+            "check": {"sampled_segments_equal_numpy_sort": bool(ok)}, "gpu_launches": 2 * args.steps}
+
+
+class PlainRunner:
+    """Times plain device-pointer sorts of one configuration at a time on one context, with the
+    keys resident in HBM: buffers are sized once for the largest configuration; the seeded input
+    is generated into pinned host memory and copied to a pristine device copy, which is copied
+    over the sort's buffer before every step, outside the timed interval."""
+
+    def __init__(self, gqs_ctypes, local, rank, max_bytes, variant):
+        import torch
+        self.torch = torch
+        self.gq = gqs_ctypes
+        self.rank = rank
+        self.host_in = torch.empty(max_bytes, dtype=torch.uint8, pin_memory=True)
+        self.host_out = torch.empty(max_bytes, dtype=torch.uint8, pin_memory=True)
+        self.pristine = torch.empty(max_bytes, dtype=torch.uint8, device="cuda")
+        self.d = torch.empty(max_bytes, dtype=torch.uint8, device="cuda")
+        self.dn = torch.empty(max_bytes, dtype=torch.uint8, device="cuda")
+        self.flush = None
+        self.ctx = gqs_ctypes.Context(device=local, sync=False, timing=True, variant=variant)
+        self.stream = torch.cuda.current_stream()
+
+    def host_view(self, buf, dtype, n):
+        return buf.numpy()[: n * np.dtype(self.gq.NP_DTYPES[dtype]).itemsize].view(self.gq.NP_DTYPES[dtype])
+
+    def prepare(self, dtype, dist, n, seed):
+        hv = self.host_view(self.host_in, dtype, n)
+        self.gq.generate(dtype, dist, seed, n, out=hv)
+        nb = hv.nbytes
+        self.pristine[:nb].copy_(self.host_in[:nb], non_blocking=False)
+        return hv
+
+    def sort_once(self, dtype, n):
+        rc = self.ctx.sort_dev(dtype, self.d.data_ptr(), self.dn.data_ptr(), n, self.stream.cuda_stream)
+        if rc != 0:
+            raise RuntimeError(f"sort enqueue failed: {self.gq.STATUS.get(rc, rc)}")
+
+    def run(self, dtype, dist, log2n, warmup, steps, clocks, seed, min_time_s=0.0, torch_check=False,
+            barrier=lambda: None):
+        """Warm-up sorts, the bit-exact check of the last one, then `steps` timed sorts (more when
+        min_time_s asks for a longer timed region). Returns the timings and the check."""
+        torch = self.torch
+        n = 1 << log2n
+        esize = np.dtype(self.gq.NP_DTYPES[dtype]).itemsize
+        nb = n * esize
+        hv = self.prepare(dtype, dist, n, seed)
+        # inputs smaller than twice the L2 are timed after an L2 flush (a 256 MiB write) per step
+        if nb < 2 * L2_BYTES and self.flush is None:
+            self.flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+        flush = self.flush if nb < 2 * L2_BYTES else None
+        warm_ms = []
+        for _ in range(warmup):
+            self.d[:nb].copy_(self.pristine[:nb])
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(self.stream)
+            self.sort_once(dtype, n)
+            e1.record(self.stream)
+            st = self.ctx.stats()
+            if st["status"] != 0:
+                raise RuntimeError(f"sort failed: {st}")
+            warm_ms.append(e0.elapsed_time(e1))
+        torch.cuda.synchronize()
+        # bit-exact check of the last warm-up result, outside any timed interval
+        self.host_out[:nb].copy_(self.d[:nb])
+        out = self.host_view(self.host_out, dtype, n)
+        check = golden_check(golden_case(dtype, dist, n, seed), hv, out)
+        if torch_check:
+            tdt = {"u32": torch.int32, "f32": torch.float32, "f64": torch.float64}[dtype]
+            src, got = self.pristine[:nb].view(tdt), self.d[:nb].view(tdt)
+            if dtype == "u32":
+                got, ref = got.to(torch.int64) & 0xFFFFFFFF, torch.sort(src.to(torch.int64) & 0xFFFFFFFF).values
+            else:
+                ref = torch.sort(src).values
+            check["bit_exact_vs_torch_sort"] = bool(torch.equal(got, ref))
+            del got, ref
+            torch.cuda.empty_cache()
+        if min_time_s > 0 and warm_ms:
+            steps = min(400, max(steps, math.ceil(min_time_s / (min(warm_ms) / 1e3))))
+        ev0 = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+        ev1 = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+        kernel_ms, algo_bytes, st = [], [], None
+        barrier()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for i in range(steps):
+            self.d[:nb].copy_(self.pristine[:nb])
+            if flush is not None:
+                flush.zero_()
+            ev0[i].record(self.stream)
+            self.sort_once(dtype, n)
+            ev1[i].record(self.stream)
+            st = self.ctx.stats()  # waits for this sort; kernel time from events on the launching stream
+            if st["status"] != 0:
+                raise RuntimeError(f"sort failed: {st}")
+            kernel_ms.append(st["kernel_ms"])
+            algo_bytes.append(st["algo_bytes"])
+        torch.cuda.synchronize()
+        barrier()
+        t1 = time.perf_counter()
+        step_ms = [a.elapsed_time(b) for a, b in zip(ev0, ev1)]
+        return {"n": n, "esize": esize, "steps": steps, "step_ms": step_ms, "kernel_ms": kernel_ms,
+                "algo_bytes": algo_bytes, "stats": st, "check": check, "t0": t0, "t1": t1, "hv": hv,
+                "clocks": clocks.window(t0, t1) if clocks else None,
+                "l2": ("inputs larger than L2 (keys rewritten from a pristine copy before every step)"
+                       if flush is None else "L2 flushed before every step (256 MiB write)")}
+
+
+def roofline_of(r, peak, peak_src, traffic=None):
+    km = float(np.mean(r["kernel_ms"]))
+    ab = float(np.mean(r["algo_bytes"]))
+    achieved = ab / (km / 1e3) / 1e9
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": traffic, "kernel": "gqs::persistent_kernel", "kernel_ms": km, "algo_bytes_per_launch": ab,
+            "peak_source": peak_src,
+            "per_unit": f"{r['esize']} B x 2 per key per pass (partition chunks + on-chip sort + register sort)"}
+
+
+PLAIN_CONFIGS = [
+    ("u32", "uniform", 20),
+    ("u32", "sorted", 28),
+    ("u32", "reverse", 28),
+    ("u32", "distinct16", 28),
+    ("u32", "zipf", 28),
+    ("u32", "gaussian", 28),
+    ("f32", "gaussian", 27),
+    ("f64", "uniform", 26),
+]
+
+
+def run_configs(args, runner, clocks, peak, peak_src):
+    """Every configuration of the benchmark other than the headline, one entry each."""
+    out = []
+    for dtype, dist, log2n in PLAIN_CONFIGS:
+        r = runner.run(dtype, dist, log2n, warmup=max(3, args.warmup), steps=max(5, args.steps), clocks=clocks,
+                       seed=SEED, min_time_s=0.25)
+        t = sum(r["step_ms"]) / 1e3
+        rf = roofline_of(r, peak, peak_src)
+        st = r["stats"]
+        v = runner.gq.variants(dtype)[st["variant"]]
+        out.append({"workload": f"plain sort, 2^{log2n} {dtype} keys, {dist}", "dtype": dtype, "dist": dist,
+                    "keys": r["n"], "value": r["n"] * r["steps"] / t / 1e9, "unit": "Gkeys/s",
+                    "ms_per_step": 1e3 * t / r["steps"], "steps": r["steps"], "kernel_ms": rf["kernel_ms"],
+                    "roofline": {"achieved": rf["achieved"], "frac": rf["frac"], "peak": peak,
+                                 "algo_bytes_per_launch": rf["algo_bytes_per_launch"]},
+                    "passes_per_key": (st["part_keys"] + st["local_keys"] + st["tiny_keys"]) / r["n"],
+                    "variant": v["name"], "check": r["check"], "clocks": r["clocks"], "l2": r["l2"]})
+    return out
 
 
 def main():
@@ -653,129 +1013,83 @@ def main():
             dist.destroy_process_group()
         return
 
-    tdt = {"u32": torch.int32, "f32": torch.float32, "f64": torch.float64}[args.dtype]
     npdt = gqs_ctypes.NP_DTYPES[args.dtype]
     esize = np.dtype(npdt).itemsize
+    peak, peak_src = measured_peak()
 
-    # ---- input
-    offsets = None
-    nseg = 1
     if args.config == "tiles":
-        nseg = (1 << args.log2n) // 8000
-        off = np.arange(nseg + 1, dtype=np.int64) * (6000 if args.dtype == "f64" else 8000)
-        n = int(off[-1])
-        offsets = torch.from_numpy(off).cuda()
-    else:
-        n = 1 << args.log2n
-    host_in = torch.empty(n, dtype=tdt, pin_memory=True)
-    hv = host_in.numpy().view(npdt) if args.dtype == "u32" else host_in.numpy()
-    gqs_ctypes.generate(args.dtype, args.dist, SEED + rank, n, out=hv)
-    pristine = host_in.cuda()
-    d = torch.empty_like(pristine)
-    dn = torch.empty_like(pristine)
-
-    ctx = gqs_ctypes.Context(device=local, sync=False, timing=True, variant=args.variant)
-    stream = torch.cuda.current_stream()
-
-    def sort_once():
-        if offsets is None:
-            rc = ctx.sort_dev(args.dtype, d.data_ptr(), dn.data_ptr(), n, stream.cuda_stream)
-        else:
-            rc = ctx.sort_segments_dev(args.dtype, d.data_ptr(), dn.data_ptr(), n, offsets.data_ptr(), nseg,
-                                       stream.cuda_stream)
-        if rc != 0:
-            raise RuntimeError(f"sort enqueue failed: {gqs_ctypes.STATUS.get(rc, rc)}")
-
-    # clocks are sampled from the warm-up on (the sampler needs ~0.2 s to start), through the
-    # timed steps
-    clocks = ClockSampler(enabled=(not args.no_clocks and rank == 0), index=local)
-    for _ in range(args.warmup):
-        d.copy_(pristine)
-        sort_once()
-        st = ctx.stats()
-        if st["status"] != 0:
-            raise RuntimeError(f"sort failed: {st}")
-    torch.cuda.synchronize()
-
-    # correctness of the warm-up result (outside any timed interval)
-    check = {}
-    if offsets is None:
-        if args.dtype == "u32":
-            got = d.to(torch.int64) & 0xFFFFFFFF
-            ref = torch.sort(pristine.to(torch.int64) & 0xFFFFFFFF).values
-        else:
-            got, ref = d, torch.sort(pristine).values
-        check["bit_exact_vs_torch_sort"] = bool(torch.equal(got, ref))
-        del got, ref
-    torch.cuda.empty_cache()
-
-    ev0 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ev1 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    kernel_ms, algo_bytes, stats_last = [], [], None
-    barrier()
-    torch.cuda.synchronize()
-    wall0 = time.perf_counter()
-    for i in range(args.steps):
-        d.copy_(pristine)
-        ev0[i].record(stream)
-        sort_once()
-        ev1[i].record(stream)
-        st = ctx.stats()  # waits for this sort; kernel time from events on the launching stream
-        if st["status"] != 0:
-            raise RuntimeError(f"sort failed: {st}")
-        kernel_ms.append(st["kernel_ms"])
-        algo_bytes.append(st["algo_bytes"])
-        stats_last = st
-    torch.cuda.synchronize()
-    barrier()
-    wall = time.perf_counter() - wall0
-    clk = clocks.stop()
-    step_ms = [a.elapsed_time(b) for a, b in zip(ev0, ev1)]
-    t_sort = max_over_ranks(sum(step_ms) / 1e3, dist)
-    value = n * world * args.steps / t_sort / 1e9
-
-    # ---- end to end through the host-pointer call
-    e2e = None
-    if not args.no_e2e and offsets is None:
-        work = torch.empty_like(host_in, pin_memory=True)
-        wv = work.numpy().view(npdt) if args.dtype == "u32" else work.numpy()
-        for _ in range(max(1, min(args.warmup, 2))):
-            work.copy_(host_in)
-            ctx.sort(wv)
-        times = []
-        for _ in range(args.steps):
-            work.copy_(host_in)
-            t0 = time.perf_counter()
-            ctx.sort(wv)
-            times.append(time.perf_counter() - t0)
-        tsum = max_over_ranks(sum(times), dist)
-        e2e = {"value": n * world * args.steps / tsum / 1e9, "unit": "Gkeys/s",
-               "h2d_bytes_per_step": n * esize, "d2h_bytes_per_step": n * esize,
-               "ms_per_step": 1e3 * tsum / args.steps, "api": "gqs_sort_" + args.dtype + " (host pointers, pinned)"}
-
-    if rank != 0:
-        ctx.close()
+        print(json.dumps(run_tiles(args, gqs_ctypes, rank, local, world, dist, barrier, peak, peak_src)), flush=True)
         if dist is not None:
             dist.destroy_process_group()
         return
 
-    peak, peak_src = measured_peak()
-    km = float(np.mean(kernel_ms))
-    ab = float(np.mean(algo_bytes))
-    achieved = ab / (km / 1e3) / 1e9
-    wkey = f"plain_{args.dtype}_{args.dist}_2^{args.log2n}" if offsets is None else f"{args.config}_{args.dtype}"
-    traffic = ncu_traffic(wkey)
-    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": traffic, "kernel": "gqs::persistent_kernel", "kernel_ms": km,
-                "algo_bytes_per_launch": ab, "peak_source": peak_src,
-                "per_unit": f"{esize} B x 2 per key per pass (partition chunks + on-chip sort + register sort)"}
+    n = 1 << args.log2n
+    want_configs = (not args.no_configs and world == 1 and args.dtype == "u32" and args.dist == "uniform"
+                    and args.log2n == 28)
+    max_bytes = n * esize
+    if want_configs:
+        max_bytes = max(max_bytes, max((1 << l2n) * np.dtype(gqs_ctypes.NP_DTYPES[t]).itemsize
+                                       for t, _, l2n in PLAIN_CONFIGS))
+    runner = PlainRunner(gqs_ctypes, local, rank, max_bytes, args.variant)
+    # clocks are sampled from before the warm-up on, through every timed region
+    clocks = ClockSampler(enabled=(not args.no_clocks and rank == 0), index=local)
+    clocks.ready()
+    r = runner.run(args.dtype, args.dist, args.log2n, args.warmup, args.steps, clocks, seed=SEED + rank,
+                   torch_check=True, barrier=barrier)
+    t_sort = max_over_ranks(sum(r["step_ms"]) / 1e3, dist)
+    value = n * world * args.steps / t_sort / 1e9
+    stats_last = r["stats"]
+    phases = runner.ctx.phases()
+
+    # ---- end to end through the host-pointer call
+    e2e = None
+    if not args.no_e2e:
+        import torch as _t
+        work = _t.empty(n * esize, dtype=_t.uint8, pin_memory=True)
+        wv = work.numpy().view(npdt)
+        for _ in range(max(1, min(args.warmup, 2))):
+            np.copyto(wv, r["hv"])
+            runner.ctx.sort(wv)
+        times = []
+        for _ in range(args.steps):
+            np.copyto(wv, r["hv"])
+            t0 = time.perf_counter()
+            runner.ctx.sort(wv)
+            times.append(time.perf_counter() - t0)
+        tsum = max_over_ranks(sum(times), dist)
+        e2e = {"value": n * world * args.steps / tsum / 1e9, "unit": "Gkeys/s",
+               "h2d_bytes_per_step": n * esize, "d2h_bytes_per_step": n * esize,
+               "ms_per_step": 1e3 * tsum / args.steps, "api": "gqs_sort_" + args.dtype + " (host pointers, pinned)",
+               "check": golden_check(golden_case(args.dtype, args.dist, n, SEED + rank), r["hv"], wv)}
+        del work
+
+    if rank != 0:
+        runner.ctx.close()
+        if dist is not None:
+            dist.destroy_process_group()
+        return
+
+    wkey = f"plain_{args.dtype}_{args.dist}_2^{args.log2n}"
+    roofline = roofline_of(r, peak, peak_src, ncu_traffic(wkey))
     cpu = None if args.no_cpu else cpu_baseline(args, n)
     v0 = gqs_ctypes.variants(args.dtype)[stats_last["variant"]]
+    configs = None
+    if want_configs:
+        configs = run_configs(args, runner, clocks, peak, peak_src)
+    prof = runner.ctx.profile() if args.profile else None
+    levels = runner.ctx.levels() if args.profile else None
+    runner.ctx.close()
+    del runner
+    import torch as _t
+    _t.cuda.empty_cache()
+    if want_configs:
+        configs.append(run_batched(args, gqs_ctypes, rank, local, world, dist, barrier, clocks=clocks,
+                                   steps=max(5, min(args.steps, 10)), warmup=3))
+    clk = r["clocks"]
     serve = None
     if args.config == "plain" and args.serve_requests > 0 and world == 1:
-        del d, dn, pristine
-        torch.cuda.empty_cache()
         serve = run_serve(args, gqs_ctypes)
+    clocks.stop()
     line = {
         "metric": METRIC if (args.config == "plain" and args.log2n == 28 and args.dtype == "u32")
         else f"Gkeys/s ({workload_name(args, n)})",
@@ -783,25 +1097,25 @@ def main():
         "ms_per_step": 1e3 * t_sort / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": args.dtype, "data": "synthetic (seeded generator, gpu-quicksort_gb300/workload)",
         "config": {"workload": workload_name(args, n), "keys": n, "distribution": args.dist, "seed": SEED,
-                   "l2": "inputs larger than L2 (keys rewritten from a pristine copy before every step)",
-                   "variant": v0["name"], "grid": stats_last["grid"], "threads": stats_last["threads"],
-                   "parallelism": f"replicas x{world}"},
+                   "l2": r["l2"], "variant": v0["name"], "grid": stats_last["grid"],
+                   "threads": stats_last["threads"], "parallelism": f"replicas x{world}"},
         "roofline": roofline,
         "cpu_baseline": cpu,
         "e2e": e2e,
         "gpu_launches": 2 * args.steps,
         "clocks": clk,
-        "check": check,
+        "check": r["check"],
         "stats": {k: stats_last[k] for k in ("part_keys", "local_keys", "tiny_keys", "fill_keys", "chunks",
                                              "part_jobs", "local_jobs", "fill_chunks", "max_depth")},
         "passes_per_key": (stats_last["part_keys"] + stats_last["local_keys"] + stats_last["tiny_keys"]) / n,
+        "phases": phases,
+        "configs": configs,
         "serve": serve,
-        "profile": ctx.profile() if args.profile else None,
-        "levels": ctx.levels() if args.profile else None,
-        "wall_s": wall,
+        "profile": prof,
+        "levels": levels,
+        "wall_s": r["t1"] - r["t0"],
     }
     print(json.dumps(line), flush=True)
-    ctx.close()
     if dist is not None:
         dist.destroy_process_group()
 

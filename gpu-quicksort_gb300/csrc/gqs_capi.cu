@@ -112,6 +112,7 @@ struct gqs_ctx {
   unsigned long long pending_keys = 0;
   gqs_stats last{};
   uint64_t last_prof[32] = {};
+  uint64_t last_phase[4] = {};  // the last sort's Queue::phase
 #ifdef GQS_PROFILE
   unsigned long long last_lvl[gqs::kLevels][6] = {};  // per-level rows of the last sort
   unsigned long long last_lvl_start = 0;
@@ -154,6 +155,7 @@ gqs_status wait_pending_locked(gqs_ctx* c) {
   }
   c->last = s;
   for (int i = 0; i < 32; ++i) c->last_prof[i] = c->q_host->prof[i];
+  for (int i = 0; i < 4; ++i) c->last_phase[i] = c->q_host->phase[i];
 #ifdef GQS_PROFILE
   std::memcpy(c->last_lvl, c->q_host->lvl, sizeof(c->last_lvl));
   c->last_lvl_start = c->q_host->lvl_start;
@@ -166,6 +168,10 @@ gqs_status wait_pending_locked(gqs_ctx* c) {
 gqs_status drain(gqs_ctx* c, gqs_status st) {
   cudaStreamSynchronize(c->copy_stream);
   cudaStreamSynchronize(c->stream);
+  (void)cudaGetLastError();
+  // A sort enqueued before the failure has run (or still runs on a caller's stream): collect it
+  // now, so that the next call neither reports its status as its own nor skips waiting for it.
+  (void)wait_pending_locked(c);
   (void)cudaGetLastError();
   return st;
 }
@@ -280,6 +286,7 @@ __global__ void accumulate_queue(const gqs::Queue* __restrict__ q, gqs::Queue* _
   acc->local_jobs += q->local_jobs;
   acc->fill_jobs += q->fill_jobs;
   if (q->max_depth > acc->max_depth) acc->max_depth = q->max_depth;
+  for (int i = 0; i < 4; ++i) acc->phase[i] += q->phase[i];
   if (q->error && !acc->error) {
     acc->error = q->error;
     acc->error_info = q->error_info;
@@ -825,6 +832,18 @@ int gqs_last_profile(gqs_ctx* c, uint64_t* out, size_t n) {
   const size_t k = n < 32 ? n : 32;
   for (size_t i = 0; i < k; ++i) out[i] = c->last_prof[i];
   return (int)k;
+}
+
+gqs_status gqs_last_phases(gqs_ctx* c, gqs_phases* out) {
+  if (!c || !out) return GQS_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(c->mu);
+  DeviceGuard dg(c->device);
+  const gqs_status st = wait_pending_locked(c);
+  out->partition_cycles = c->last_phase[0];
+  out->onchip_cycles = c->last_phase[1];
+  out->fill_cycles = c->last_phase[2];
+  out->total_cycles = c->last_phase[3];
+  return st;
 }
 
 int gqs_last_levels(gqs_ctx* c, gqs_level* out, int max) {

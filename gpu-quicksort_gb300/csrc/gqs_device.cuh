@@ -62,6 +62,10 @@ struct Queue {
   unsigned long long error_info;
   unsigned long long part_keys, local_keys, tiny_keys, fill_keys, chunks;
   uint32_t part_jobs, local_jobs, fill_jobs, max_depth;
+  // Cycles of each CTA's consumer leader thread, summed over CTAs, by the item it worked on:
+  // partition chunk iterations, on-chip sorts (tile wait, sort, write-out), queued pivot-run
+  // fills, and the whole consumer loop (the rest is waiting for items and draining).
+  unsigned long long phase[4];
   unsigned long long prof[32];  // cycle counters of a -DGQS_PROFILE build (zero otherwise)
 #ifdef GQS_PROFILE
   // Per partition level (job depth; the last row takes every deeper level) in a -DGQS_PROFILE
@@ -241,6 +245,7 @@ struct alignas(128) Smem {
   uint32_t wlt[3][C::NCW], wgt[3][C::NCW];  // per-warp totals: count (k), scatter (k-1), free (k-2)
   uint32_t cq[C::CQ];
   uint32_t cq_head, cq_tail, term, cons_ok, lok;
+  unsigned long long ph[5];  // consumer leader's phase cycles: partition, on-chip, fill; item start; loop start
   // output-range reservations: consumer leader -> reserver warp -> consumers
   uint32_t rq_job[C::RQ], rq_ls[C::RQ], rq_gs[C::RQ], rs_done[C::RQ];
   unsigned long long rs_lb[C::RQ], rs_gb[C::RQ];
@@ -1532,6 +1537,12 @@ struct Persistent {
 #endif
     unsigned long long st_part = 0, st_local = 0, st_chunks = 0;
     uint32_t st_local_jobs = 0, st_fill_jobs = 0;
+    // Leader cycles by item kind (Queue::phase), kept in shared memory by thread 0 alone, so that
+    // no register is held across the loop for them.
+    if (tid == 0) {
+      sm.ph[0] = sm.ph[1] = sm.ph[2] = 0ull;
+      sm.ph[4] = (unsigned long long)clock64();
+    }
     GQS_PROF_DECL
     GQS_PROF_T(t_all)
 
@@ -1539,6 +1550,7 @@ struct Persistent {
     cbar();
     for (;;) {
       if (!sm.cons_ok) break;
+      if (tid == 0) sm.ph[3] = (unsigned long long)clock64();
       GQS_PROF_T(t_it)
       GQS_PROF_CNT(PF_N_ITEMS, 1)
       const uint32_t s = k % C::STAGES;
@@ -1640,6 +1652,7 @@ struct Persistent {
         ++npart;
         ++k;
         GQS_PROF_ADD(PF_C_PART, t_it)
+        if (tid == 0) sm.ph[0] += (unsigned long long)clock64() - sm.ph[3];
         continue;
       }
 
@@ -1665,6 +1678,7 @@ struct Persistent {
       GQS_PROF_ADD(PF_C_DRAIN, t_it)
 
       if (dd.kind == ITEM_TERM) break;
+      if (tid == 0) sm.ph[3] = (unsigned long long)clock64();
       if (dd.kind == ITEM_FILL) {
         // Queued pivot-run fill: write the raw pivot over d[gbeg, gbeg + len).
         GQS_PROF_T(tf)
@@ -1675,6 +1689,7 @@ struct Persistent {
         ++st_fill_jobs;
         GQS_PROF_ADD(PF_C_FILL, tf)
         if (tid == 0) atomicAdd(&a.q->done, (unsigned long long)dd.len);
+        if (tid == 0) sm.ph[2] += (unsigned long long)clock64() - sm.ph[3];
       } else if (dd.kind == ITEM_LOCAL) {
         GQS_PROF_T(tl)
         if (tid == 0) sm.lok = mbar_wait(&sm.lfull, nloc & 1u, a.q, a.timeout_ns, 7) ? 1u : 0u;
@@ -1746,6 +1761,7 @@ struct Persistent {
         st_local += m;
         ++st_local_jobs;
         ++nloc;
+        if (tid == 0) sm.ph[1] += (unsigned long long)clock64() - sm.ph[3];
       }
       // ITEM_FLUSH needs nothing beyond the drain above.
       if (tid == 0) leader_wait_slot(a, sm, k + 1);
@@ -1762,6 +1778,10 @@ struct Persistent {
       if (st_chunks) atomicAdd(&a.q->chunks, st_chunks);
       if (st_local_jobs) atomicAdd(&a.q->local_jobs, st_local_jobs);
       if (st_fill_jobs) atomicAdd(&a.q->fill_jobs, st_fill_jobs);
+      atomicAdd(&a.q->phase[0], sm.ph[0]);
+      atomicAdd(&a.q->phase[1], sm.ph[1]);
+      atomicAdd(&a.q->phase[2], sm.ph[2]);
+      atomicAdd(&a.q->phase[3], (unsigned long long)clock64() - sm.ph[4]);
     }
   }
 };

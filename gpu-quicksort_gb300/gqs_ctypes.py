@@ -31,7 +31,8 @@ EXPORTS = [
     "gqs_sort_u32_dev", "gqs_sort_f32_dev", "gqs_sort_f64_dev",
     "gqs_sort_segments_u32_dev", "gqs_sort_segments_f32_dev", "gqs_sort_segments_f64_dev",
     "gqs_sort_segments_u32", "gqs_sort_segments_f32", "gqs_sort_segments_f64",
-    "gqs_sort_u32_noalloc", "gqs_sync", "gqs_last_stats", "gqs_last_profile", "gqs_last_levels", "gqs_variant_count", "gqs_variant_describe", "gqs_set_variant",
+    "gqs_sort_u32_noalloc", "gqs_sync", "gqs_last_stats", "gqs_last_profile", "gqs_last_levels",
+    "gqs_last_phases", "gqs_variant_count", "gqs_variant_describe", "gqs_set_variant",
     "gqs_get_variant", "gqs_strerror", "gqs_version",
     "gqs_batch_create", "gqs_batch_destroy", "gqs_batch_keys", "gqs_batch_offsets", "gqs_batch_launch",
     "gqs_batch_wait", "gqs_batch_copy_in", "gqs_batch_copy_out", "gqs_batch_set_variant", "gqs_batch_get_variant", "gqs_batch_autotune",
@@ -70,6 +71,11 @@ class Level(C.Structure):
     _fields_ = [("depth", C.c_uint32), ("part_jobs", C.c_uint32), ("part_keys", C.c_uint64),
                 ("local_jobs", C.c_uint32), ("reserved", C.c_uint32), ("local_keys", C.c_uint64),
                 ("first_ms", C.c_double), ("last_ms", C.c_double)]
+
+
+class Phases(C.Structure):
+    _fields_ = [("partition_cycles", C.c_uint64), ("onchip_cycles", C.c_uint64), ("fill_cycles", C.c_uint64),
+                ("total_cycles", C.c_uint64)]
 
 
 class VariantDesc(C.Structure):
@@ -154,6 +160,8 @@ def load_library(path: str | None = None) -> C.CDLL:
     lib.gqs_last_profile.restype = C.c_int
     lib.gqs_last_levels.argtypes = [vp, C.POINTER(Level), C.c_int]
     lib.gqs_last_levels.restype = C.c_int
+    lib.gqs_last_phases.argtypes = [vp, C.POINTER(Phases)]
+    lib.gqs_last_phases.restype = st
     lib.gqs_variant_count.argtypes = [C.c_int]
     lib.gqs_variant_count.restype = C.c_int
     lib.gqs_variant_describe.argtypes = [C.c_int, C.c_int, C.POINTER(VariantDesc)]
@@ -322,6 +330,18 @@ class Context:
         buf = (C.c_uint64 * 32)()
         k = self.lib.gqs_last_profile(self.h, buf, 32)
         return {name: int(buf[i]) for i, name in enumerate(self.PROFILE_SLOTS) if i < k}
+
+    def phases(self) -> dict:
+        """The last sort's split of consumer-leader cycles: partition chunks, on-chip sorts, pivot
+        fills and the whole loop, with the shares of the first three."""
+        ph = Phases()
+        _check(self.lib.gqs_last_phases(self.h, C.byref(ph)), "gqs_last_phases")
+        d = {f: int(getattr(ph, f)) for f, _ in Phases._fields_}
+        tot = d["total_cycles"] or 1
+        d["partition_share"] = d["partition_cycles"] / tot
+        d["onchip_share"] = d["onchip_cycles"] / tot
+        d["fill_share"] = d["fill_cycles"] / tot
+        return d
 
     def set_variant(self, dtype: str, v: int) -> None:
         _check(self.lib.gqs_set_variant(self.h, DTYPES[dtype], v), "gqs_set_variant")

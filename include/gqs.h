@@ -145,8 +145,13 @@ gqs_status gqs_sort_pairs_f32_dev(gqs_ctx* ctx, float* keys, uint32_t* values, s
  * before any work. All of its scratch is one static device array inside the library (about
  * 6 MB, held by every GPU that loads the library until the process exits) shared by every call:
  * calls that overlap on the GPU race, so the caller serialises them. The first call on a device
- * looks up that array's address and prepares the kernel; make it before any stream capture.
- * No counterpart in the reference, which allocates its buffers per call. */
+ * looks up that array's address and prepares the kernel. Every call blocks: it reads the
+ * status block back and synchronises `stream` before it returns, so it must never be made on a
+ * stream that is being captured into a CUDA graph. The device-side no-progress limit is fixed
+ * at 4 s (there is no context to configure it): a sort that stalls returns GQS_ERR_TIMEOUT after
+ * about 4 s, and the static array then still holds that call's partial state, which the next
+ * call clears before it starts. No counterpart in the reference, which allocates its buffers
+ * per call. */
 gqs_status gqs_sort_u32_noalloc(uint32_t* d, size_t n, void* stream);
 
 /* ---- Batched sort, captured once as a CUDA graph ------------------------------------------
@@ -286,6 +291,22 @@ gqs_status gqs_last_stats(gqs_ctx* ctx, gqs_stats* out);
 /* Per-role cycle counters of the last sort, filled only by a library built with -DGQS_PROFILE
  * (zeros otherwise). Writes up to n values and returns the number written. */
 int gqs_last_profile(gqs_ctx* ctx, uint64_t* out, size_t n);
+
+/* Where the last sort's persistent kernel spent its time, on the clock of each CTA's consumer
+ * leader thread (SM cycles, summed over CTAs): partition chunk iterations (the gqsort_kernel
+ * counterpart), on-chip sorts of ranges of at most one tile (the lqsort_kernel counterpart:
+ * tile wait, sort, write-out), writes of queued pivot runs, and the whole consumer loop; the
+ * remainder of total_cycles is waiting for work and draining the chunk pipeline. Recorded by
+ * every build (a few clock reads per work item). */
+typedef struct gqs_phases {
+  uint64_t partition_cycles;
+  uint64_t onchip_cycles;
+  uint64_t fill_cycles;
+  uint64_t total_cycles;
+} gqs_phases;
+
+/* The phase split of the context's last sort (waits for it if it is still running). */
+gqs_status gqs_last_phases(gqs_ctx* ctx, gqs_phases* out);
 
 /* One partition level (job depth; the root job is depth 0) of the last sort. */
 typedef struct gqs_level {

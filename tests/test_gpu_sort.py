@@ -1,9 +1,9 @@
 """GPU parity: the CUDA sort through the C ABI against the oracle, bit for bit.
 
 Small and medium sizes compare with std::sort (the reference's verifier, run by the oracle
-library) and with the committed golden vectors; full configuration sizes compare with an
-independent GPU sort (torch.sort) and check size-independent properties (sortedness, a
-permutation-invariant checksum).
+library) and with the committed golden vectors; every benchmark configuration at its full size
+compares with std::sort through committed SHA-256 digests of its output (and with torch.sort);
+the largest arrays compare with torch.sort and check sortedness.
 """
 import hashlib
 import json
@@ -184,31 +184,96 @@ def test_async_calls_then_sync():
 
 
 # ---------------------------------------------------------------------------
-# full configuration sizes: exact comparison with an independent GPU sort
+# full configuration sizes: bit-exact against std::sort, through its committed digests
 
-FULL = [("u32", d, 1 << 28) for d in ("uniform", "sorted", "reverse", "distinct16", "zipf", "gaussian")] + [
-    ("f32", "gaussian", 1 << 27), ("f64", "uniform", 1 << 26)]
+FULL_SIZE = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "full_size.json")))
+FULL = [c for c in FULL_SIZE["cases"] if c["kind"] == "plain"]
 
 
-@pytest.mark.parametrize("dtype,dist,n", FULL, ids=lambda x: str(x))
-def test_full_size_configs(gpu_ctx, dtype, dist, n):
+def _device_sort_and_digest(gpu_ctx, dtype, a):
+    """Sorts a copy of host array `a` through the device-pointer C ABI call; returns the result
+    on the host, and torch.sort's result as a second, independent check."""
     torch = _torch()
-    a = gqs_ctypes.generate(dtype, dist, 2026, n)
-    if dtype == "u32":
-        t = torch.from_numpy(a.view(np.int32)).cuda()
-        ref = torch.sort(t.to(torch.int64) & 0xFFFFFFFF).values
-    else:
-        t = torch.from_numpy(a).cuda()
-        ref = torch.sort(t).values
+    n = a.size
+    t = torch.from_numpy(a.view(np.int32) if dtype == "u32" else a).cuda()
+    ref = torch.sort(t.to(torch.int64) & 0xFFFFFFFF).values if dtype == "u32" else torch.sort(t).values
     assert gpu_ctx.sort_dev(dtype, t.data_ptr(), None, n, torch.cuda.current_stream().cuda_stream) == 0
     got = (t.to(torch.int64) & 0xFFFFFFFF) if dtype == "u32" else t
-    assert torch.equal(got, ref)
-    # size-independent properties on top of the exact comparison
-    assert bool((got[1:] >= got[:-1]).all())
-    st = gpu_ctx.stats()
-    assert st["status"] == 0 and st["keys"] == n
+    same_as_torch = bool(torch.equal(got, ref))
+    out = t.cpu().numpy()
     del t, ref, got
     torch.cuda.empty_cache()
+    return (out.view(np.uint32) if dtype == "u32" else out), same_as_torch
+
+
+@pytest.mark.parametrize("case", FULL, ids=lambda c: f"{c['dtype']}-{c['dist']}-{c['n']}")
+def test_full_size_configs(gpu_ctx, case):
+    """Every plain configuration of the benchmark at its real size (2^28 u32 in six
+    distributions, 2^27 f32, 2^26 f64, and 2^20 u32), on the benchmark's own seeded input: the
+    output's SHA-256 equals that of std::sort's output (the reference's verifier,
+    GPU-Quicksort_Full_SYCL/QuicksortMain.cpp:1120-1138), recorded on the CPU by
+    tests/golden/make_full_size.py."""
+    dtype, n = case["dtype"], case["n"]
+    a = gqs_ctypes.generate(dtype, case["dist"], case["seed"], n)
+    assert sha(a) == case["input_sha256"], "the generator is not the one the digests were made with"
+    out, same_as_torch = _device_sort_and_digest(gpu_ctx, dtype, a)
+    assert sha(out) == case["sorted_sha256"]
+    assert out[:4].tobytes().hex() == case["head"] and out[-4:].tobytes().hex() == case["tail"]
+    assert same_as_torch
+    st = gpu_ctx.stats()
+    assert st["status"] == 0 and st["keys"] == n
+
+
+BATCH_CASE = next(c for c in FULL_SIZE["cases"] if c["kind"] == "segments")
+
+
+def _segment_digests_match(out, off, case):
+    bad = [i for i in range(len(off) - 1)
+           if hashlib.sha256(out[int(off[i]):int(off[i + 1])].tobytes()).hexdigest()[:16] != case["segment_sha256_16"][i]]
+    return bad
+
+
+def test_batched_config_graph_replay():
+    """The batched configuration at its real shape (4096 uint32 arrays, lengths log-uniform in
+    [32, 2^20], about 3.9e8 keys): autotuned, then one graph replay; every segment's digest and
+    the whole output's digest equal std::sort's."""
+    case = BATCH_CASE
+    off = gqs_ctypes.segment_offsets(case["seed"], case["segments"], case["min_len"], case["max_len"])
+    assert sha(off.astype(np.uint64)) == case["offsets_sha256"]
+    n = int(off[-1])
+    a = gqs_ctypes.generate("u32", "uniform", case["seed"], n)
+    assert sha(a) == case["input_sha256"]
+    with gqs_ctypes.Batch("u32", n, case["segments"]) as b:
+        b.set_segments(off)
+        b.copy_in(a)
+        best, ms = b.autotune(case["segments"], reps=1)
+        assert 0 <= best < len(ms)
+        b.copy_in(a)  # the autotuner leaves the keys sorted; replay on the unsorted input
+        assert b.launch(case["segments"]) == 0
+        code, st = b.wait()
+        assert code == 0 and st["keys"] == n
+        out = np.empty_like(a)
+        b.copy_out(out)
+    assert _segment_digests_match(out, off, case) == []
+    assert sha(out) == case["sorted_sha256"]
+
+
+def test_batched_config_segmented_call(gpu_ctx):
+    """The same configuration through the context's segmented device-pointer call."""
+    torch = _torch()
+    case = BATCH_CASE
+    off = gqs_ctypes.segment_offsets(case["seed"], case["segments"], case["min_len"], case["max_len"])
+    n = int(off[-1])
+    a = gqs_ctypes.generate("u32", "uniform", case["seed"], n)
+    t = torch.from_numpy(a.view(np.int32)).cuda()
+    o = torch.from_numpy(off.astype(np.int64)).cuda()
+    assert gpu_ctx.sort_segments_dev("u32", t.data_ptr(), None, n, o.data_ptr(), case["segments"],
+                                     torch.cuda.current_stream().cuda_stream) == 0
+    out = t.cpu().numpy().view(np.uint32)
+    del t, o
+    torch.cuda.empty_cache()
+    assert _segment_digests_match(out, off, case) == []
+    assert sha(out) == case["sorted_sha256"]
 
 
 # The largest arrays: the top of the reference's benchmark sweep, 2 x 16384 x 16384 = 2^29
@@ -218,7 +283,13 @@ MAXSIZE = [("u32", "uniform", 1 << 29), ("f64", "uniform", 1 << 28), ("f32", "ga
 
 @pytest.mark.parametrize("dtype,dist,n", MAXSIZE, ids=lambda x: str(x))
 def test_maximum_sizes(gpu_ctx, dtype, dist, n):
-    test_full_size_configs(gpu_ctx, dtype, dist, n)
+    """Beyond the committed digests: exact equality with torch.sort and sortedness."""
+    a = gqs_ctypes.generate(dtype, dist, 2026, n)
+    out, same_as_torch = _device_sort_and_digest(gpu_ctx, dtype, a)
+    assert same_as_torch
+    assert bool(np.all(out[1:] >= out[:-1]))
+    st = gpu_ctx.stats()
+    assert st["status"] == 0 and st["keys"] == n
 
 
 # ---------------------------------------------------------------------------

@@ -47,3 +47,12 @@ def test_noalloc_refuses_more_than_its_scratch():
     # n is checked before the pointer is used, so a small buffer is safe here
     assert lib.gqs_sort_u32_noalloc(ctypes.c_void_p(buf.data_ptr()), MAX_KEYS + 1, None) == 1
     assert lib.gqs_sort_u32_noalloc(None, 0, None) == 0
+
+
+def test_noalloc_refuses_null_and_misaligned_pointers():
+    torch = pytest.importorskip("torch")
+    lib = gqs_ctypes.load_library()
+    buf = torch.zeros(16, dtype=torch.int32, device="cuda")
+    # both are refused by the argument checks, before the device is touched
+    assert lib.gqs_sort_u32_noalloc(None, 2, None) == 1
+    assert lib.gqs_sort_u32_noalloc(ctypes.c_void_p(buf.data_ptr() + 2), 2, None) == 1
