@@ -839,7 +839,9 @@ gqs_status gqs_last_phases(gqs_ctx* c, gqs_phases* out) {
   std::lock_guard<std::mutex> lk(c->mu);
   DeviceGuard dg(c->device);
   const gqs_status st = wait_pending_locked(c);
-  out->partition_cycles = c->last_phase[0];
+  // partition chunks are not timed one by one (see Queue::phase): they are the remainder
+  const uint64_t rest = c->last_phase[1] + c->last_phase[2];
+  out->partition_cycles = c->last_phase[3] > rest ? c->last_phase[3] - rest : 0;
   out->onchip_cycles = c->last_phase[1];
   out->fill_cycles = c->last_phase[2];
   out->total_cycles = c->last_phase[3];

@@ -62,9 +62,10 @@ struct Queue {
   unsigned long long error_info;
   unsigned long long part_keys, local_keys, tiny_keys, fill_keys, chunks;
   uint32_t part_jobs, local_jobs, fill_jobs, max_depth;
-  // Cycles of each CTA's consumer leader thread, summed over CTAs, by the item it worked on:
-  // partition chunk iterations, on-chip sorts (tile wait, sort, write-out), queued pivot-run
-  // fills, and the whole consumer loop (the rest is waiting for items and draining).
+  // Cycles of each CTA's consumer leader thread, summed over CTAs: [1] on-chip sorts (tile wait,
+  // sort, write-out), [2] queued pivot-run fills, [3] the whole consumer loop; the rest of [3] is
+  // partition chunks, pipeline drains and waits for work ([0] is unused: a clock read per chunk
+  // on the leader's path cost 5 % of a large sort).
   unsigned long long phase[4];
   unsigned long long prof[32];  // cycle counters of a -DGQS_PROFILE build (zero otherwise)
 #ifdef GQS_PROFILE
@@ -177,6 +178,12 @@ struct SortArgs {
 
 // Kernel configuration. TILE keys fit one local (on-chip) sort; CHUNK keys are one staged
 // partition chunk; TINY = 32*R keys are sorted in registers by one warp.
+// Mean bucket size of the on-chip sample split, as a fraction of the register sort: TINY / 8
+// (32 u32 keys, 16 f64 keys; at most NB_MAX buckets per tile).
+#ifndef GQS_BUCKET_DIV
+#define GQS_BUCKET_DIV 8
+#endif
+
 template <class T_, int NCW_, int TILE_, int CHUNK_, int STAGES_, int R_>
 struct Cfg {
   using T = T_;
@@ -208,11 +215,16 @@ struct Cfg {
   static constexpr int NB_MAX = 256;
   static constexpr int SPLIT_MIN = 8 * TINY;
   static constexpr int SPLIT_SAMPLES = 256;
+  static constexpr int SPLIT_RUN = 32;                 // samples are sorted as runs of 32
+  static constexpr int BUCKET = TINY / GQS_BUCKET_DIV;  // mean bucket size the split aims for
+  static constexpr int NCLASS = 7;                     // bucket classes (network sizes), see sample_split
   static_assert(CHUNK % NC == 0, "chunk must be a multiple of the consumer threads");
+  static_assert(NCW >= 3 && NCW <= 32, "the partition loop's bookkeeping uses consumer warps 0, 1 and 2");
   static_assert((CHUNK * sizeof(B)) % 16 == 0, "chunk must be a multiple of 16 bytes");
   static_assert(TILE > TINY, "tile must exceed the register sort");
   static_assert(NB_MAX <= 256 && NB_MAX >= 32, "bucket labels are bytes; the scan takes 32..256 buckets");
-  static_assert(SPLIT_SAMPLES % 32 == 0 && SPLIT_SAMPLES >= NB_MAX, "samples per lane; one pivot per bucket");
+  static_assert(SPLIT_SAMPLES == 256 && NB_MAX == 256, "8 samples and 8 bucket counts per lane of one warp");
+  static_assert(SPLIT_RUN == 32 && NC >= SPLIT_SAMPLES, "runs of 32 samples, one thread per sample");
 };
 
 // A segment of the on-chip tile being partitioned slice by slice (shared memory).
@@ -244,7 +256,7 @@ struct alignas(128) Smem {
   Desc desc[C::STAGES];
   uint32_t wlt[3][C::NCW], wgt[3][C::NCW];  // per-warp totals: count (k), scatter (k-1), free (k-2)
   uint32_t cq[C::CQ];
-  uint32_t cq_head, cq_tail, term, cons_ok, lok;
+  uint32_t cq_head, cq_tail, term, cons_ok, slot_ok, lok;
   unsigned long long ph[5];  // consumer leader's phase cycles: partition, on-chip, fill; item start; loop start
   // output-range reservations: consumer leader -> reserver warp -> consumers
   uint32_t rq_job[C::RQ], rq_ls[C::RQ], rq_gs[C::RQ], rs_done[C::RQ];
@@ -255,8 +267,11 @@ struct alignas(128) Smem {
   LRec lrec[C::LREC];
   // local sort, first level: pivots, bucket counts (then cursors), bucket starts, labels
   typename C::B spl[C::NB_MAX];
-  uint32_t bcnt[C::NB_MAX];
-  uint32_t bstart[C::NB_MAX + 1];
+  alignas(16) uint32_t bcnt[C::NB_MAX];
+  alignas(16) uint32_t bstart[C::NB_MAX + 4];
+  // the buckets of each network class (appended in any order) and their numbers
+  uint8_t cls_list[C::NCLASS][C::NB_MAX];
+  uint32_t cls_cnt[8];
   uint8_t lb[C::TILE];
 };
 
@@ -341,17 +356,22 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, Queue*
 }
 
 // ---------------------------------------------------------------------------
-// Warp-level bitonic sort of 32*R keys held R per lane; network element e = lane*R + r.
-// (Replaces the reference's work-group bitonic network, QuicksortKernels.cl:40-68.)
+// Warp-level bitonic sort of NET keys held R per lane by NET / R lanes (a power of two); network
+// element e = (lane % (NET / R)) * R + r, so one warp runs 32 * R / NET networks side by side, one
+// per group of NET / R consecutive lanes (every shuffle stays inside its group). (Replaces the
+// reference's work-group bitonic network, QuicksortKernels.cl:40-68.)
 // Flip form: each merge of size k starts by comparing e with its mirror e ^ (k-1), then
 // half-cleaners compare e with e ^ j; the lower index always keeps the minimum, so no
-// compare-exchange needs a per-element direction. N independent networks run interleaved,
-// which multiplies the independent work in every stage by N (the stages are a latency chain).
-template <int R, int N, class K>
+// compare-exchange needs a per-element direction. Stages with j < R compare two registers of one
+// lane (no shuffle), so more keys per lane means fewer shuffles per key. N independent sets of
+// networks run interleaved, which multiplies the independent work in every stage by N (the
+// stages are a latency chain).
+template <int R, int N, class K, int NET = 32 * R>
 __device__ __forceinline__ void warp_bitonic_n(K (&v)[N * R]) {
+  static_assert(NET >= R && NET <= 32 * R && (NET & (NET - 1)) == 0, "a network of 1 to 32 lanes");
   const int lane = threadIdx.x & 31;
 #pragma unroll
-  for (int k = 2; k <= 32 * R; k <<= 1) {
+  for (int k = 2; k <= NET; k <<= 1) {
     if (k <= R) {
 #pragma unroll
       for (int n = 0; n < N; ++n)
@@ -1304,59 +1324,108 @@ struct Persistent {
 #endif
   }
 
+  // Sorts `cnt` buckets of class log2(G) at once: bucket cls_list[log2 G][first + g] (keys
+  // tileB[bstart[b], bstart[b+1]), at most G * R of them) is sorted by lanes [g * G, g * G + G)
+  // into A at the same place, with a network of G * R keys padded with the key maximum. Whole
+  // warp; returns the keys placed.
+  template <int G>
+  static __device__ __noinline__ uint32_t bucket_networks(Smem<C>& sm, B* A, const uint8_t* list, uint32_t cnt) {
+    constexpr int R = C::R;
+    const uint32_t lane = threadIdx.x & 31, g = lane / G, gl = lane % G;
+    uint32_t bs = 0, n = 0;
+    if (g < cnt) {
+      const uint32_t b = list[g];
+      bs = sm.bstart[b];
+      n = sm.bstart[b + 1] - bs;
+    }
+    B v[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const uint32_t e = (uint32_t)r * G + gl;  // any input layout is valid; this one spreads the banks
+      v[r] = e < n ? sm.tileB[bs + e] : kmax<B>();
+    }
+    warp_bitonic_n<R, 1, B, G * R>(v);
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const uint32_t e = gl * R + (uint32_t)r;
+      if (e < n) A[bs + e] = v[r];
+    }
+    return __reduce_add_sync(0xffffffffu, gl == 0 ? n : 0u);
+  }
+
   // First level of the on-chip sort for tiles of SPLIT_MIN keys or more: one multi-pivot
-  // partition of the whole tile. Warp 0 sorts SPLIT_SAMPLES evenly spaced keys in registers and
-  // keeps nb - 1 of them as pivots (nb a power of two, buckets of about TINY / 4 keys), stored as
-  // an implicit search tree in breadth-first order (node i has children 2i and 2i + 1), so the
-  // lanes of a warp reading one level of the tree hit distinct banks. Every consumer thread then
-  // labels its keys with their bucket (bucket b holds pivot[b-1] < key <= pivot[b]) and counts
-  // them; after an exclusive scan of the counts a second pass scatters every key into B at its
-  // bucket's place. The buckets are disjoint ranges in final order: each warp sorts its buckets
-  // into A in registers, or publishes one longer than TINY as a slice-partitioned segment. Whole
-  // CTA; returns the keys this warp finalised. (Inlined: as a called function its register
+  // partition of the whole tile into nb buckets (nb a power of two, buckets of about BUCKET keys),
+  // then every bucket sorted in registers. Whole CTA; returns the keys this warp finalised.
+  //  1. Pivots. Warp 0 sorts SPLIT_SAMPLES evenly spaced keys as runs of 32 (groups of 4 lanes,
+  //     8 samples each); every sample then finds its rank among all of them, by binary searches
+  //     in the other runs, and the sample of rank (q + 1) * (SPLIT_SAMPLES / nb) - 1 becomes
+  //     pivot q. The pivots are stored as an implicit search tree in breadth-first order (node i
+  //     has children 2i and 2i + 1), so the lanes of a warp reading one level hit distinct banks.
+  //  2. Every consumer thread labels its keys with their bucket (bucket b holds
+  //     pivot[b-1] < key <= pivot[b]) and counts them.
+  //  3. Warp 0 scans the counts (16-byte loads and stores): bucket starts, and scatter cursors.
+  //  4. Every key is scattered into tileB at its bucket's place; meanwhile each bucket is entered
+  //     in the list of its class: class c <= 5 is sorted by a group of 2^c lanes holding R keys
+  //     each (2^c * R keys at most), class 6 holds the buckets longer than TINY.
+  //  5. Tasks, dealt round robin to the warps largest class first: a class-6 bucket becomes a
+  //     slice-partitioned segment; a class-c task sorts 32 >> c buckets of that class at once.
+  // The buckets are disjoint ranges in final order. (Inlined: as a called function its register
   // demand made the kernel keep partition-loop values in local memory.)
   static __device__ __forceinline__ uint32_t sample_split(const SortArgs<T>& a, Smem<C>& sm, B* A, uint32_t m,
                                                        unsigned long long* lp) {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-#ifdef GQS_PROFILE
-    long long tp = clock64();
-#define GQS_SPLIT_STAMP(k)                                             \
-  if (tid == 0) {                                                      \
-    const long long tn = clock64();                                    \
-    lp[k] += (unsigned long long)(tn - tp);                            \
-    tp = tn;                                                           \
-  }
-#else
-#define GQS_SPLIT_STAMP(k)
-#endif
     uint32_t nb = 2, lg = 1;
-    while (nb < (uint32_t)C::NB_MAX && nb * (uint32_t)(C::TINY / 4) < m) {
+    while (nb < (uint32_t)C::NB_MAX && nb * (uint32_t)C::BUCKET < m) {
       nb <<= 1;
       ++lg;
     }
-    for (uint32_t i = tid; i < nb; i += C::NC) sm.bcnt[i] = 0u;
+    for (uint32_t i = tid; i < (uint32_t)C::NB_MAX; i += C::NC) sm.bcnt[i] = 0u;
+    if (tid < 8) sm.cls_cnt[tid] = 0u;
+    constexpr int RS = C::SPLIT_SAMPLES / 32;  // samples per lane
+    constexpr int RUN = C::SPLIT_RUN;
+    constexpr int NRUN = C::SPLIT_SAMPLES / RUN;
+    B* smp = sm.tileB;  // free until the scatter
     if (warp == 0) {
-      constexpr int RS = C::SPLIT_SAMPLES / 32;
       B v[RS];
 #pragma unroll
       for (int r = 0; r < RS; ++r)
         v[r] = A[(uint32_t)(((unsigned long long)(r * 32 + lane) * m) / (unsigned long long)C::SPLIT_SAMPLES)];
-      warp_bitonic<RS>(v);  // sample j is now v[j % RS] of lane j / RS
-      B* smp = sm.tileB;    // free until the scatter
+      // run lane / 4 holds its element (lane % 4) * RS + r in v[r]
+      warp_bitonic_n<RS, 1, B, RUN>(v);
 #pragma unroll
-      for (int r = 0; r < RS; ++r) smp[lane * RS + r] = v[r];
-      __syncwarp();
-      // Tree node i (level l = floor(log2 i), p = i - 2^l) is pivot (2p + 1) * 2^(lg-l-1) - 1 in
-      // sorted order; pivot q is sample (q + 1) * (SPLIT_SAMPLES / nb) - 1.
+      for (int r = 0; r < RS; ++r) smp[(uint32_t)lane * RS + r] = v[r];
+    }
+    cbar();
+    if (tid < C::SPLIT_SAMPLES) {
+      // The rank of sample tid: its index in its run plus, in every other run, the samples that
+      // come before it (smaller ones, and equal ones of an earlier run). All searches are
+      // independent; the one in the sample's own run is made and discarded.
+      const uint32_t g = (uint32_t)tid / RUN, i = (uint32_t)tid % RUN;
+      const B x = smp[tid];
+      uint32_t rank = 0;
+#pragma unroll
+      for (uint32_t h = 0; h < (uint32_t)NRUN; ++h) {
+        const B* run = smp + h * RUN;
+        uint32_t pos = 0;
+#pragma unroll
+        for (uint32_t st = RUN; st > 0; st >>= 1) {
+          if (pos + st <= (uint32_t)RUN) {
+            const B y = run[pos + st - 1];
+            if (h < g ? y <= x : y < x) pos += st;
+          }
+        }
+        rank += h == g ? i : pos;
+      }
+      // pivot q is the sample of rank (q + 1) * step - 1; with q1 = q + 1 = (2p + 1) << (lg - l - 1)
+      // it is tree node 2^l + p
       const uint32_t step = (uint32_t)C::SPLIT_SAMPLES / nb;
-      for (uint32_t i = 1u + (uint32_t)lane; i < nb; i += 32u) {
-        const uint32_t l = 31u - (uint32_t)__clz(i);
-        const uint32_t q = ((2u * (i - (1u << l)) + 1u) << (lg - l - 1u)) - 1u;
-        sm.spl[i] = smp[(q + 1u) * step - 1u];
+      const uint32_t q1 = (rank + 1u) / step;
+      if ((rank + 1u) % step == 0u && q1 < nb) {
+        const uint32_t tz = (uint32_t)__ffs(q1) - 1u;
+        sm.spl[(1u << (lg - 1u - tz)) + (q1 >> (tz + 1u))] = x;
       }
     }
     cbar();
-    GQS_SPLIT_STAMP(9)
     // KU keys per thread in flight: their tree walks (one dependent shared load per level) and
     // the scatter's atomic-then-store chains overlap (four 32-bit keys; two 64-bit keys, where
     // four measured slower)
@@ -1388,38 +1457,40 @@ struct Persistent {
       atomicAdd(&sm.bcnt[b - nb], 1u);
     }
     cbar();
-    GQS_SPLIT_STAMP(10)
-    if (warp == 0) {  // exclusive scan of the counts: bucket starts, and cursors for the scatter
-      constexpr int PER = C::NB_MAX / 32;
-      const uint32_t per = nb > 32u ? nb / 32u : 1u;
-      uint32_t loc[PER];
-      uint32_t sum = 0;
-#pragma unroll
-      for (int q = 0; q < PER; ++q) {
-        const uint32_t idx = (uint32_t)lane * per + (uint32_t)q;
-        const uint32_t c = ((uint32_t)q < per && idx < nb) ? sm.bcnt[idx] : 0u;
-        loc[q] = sum;
-        sum += c;
-      }
+    if (warp == 0) {
+      // lane l owns buckets 8l .. 8l + 7 (counts past nb are zero)
+      const uint4 c0 = reinterpret_cast<const uint4*>(sm.bcnt)[2 * lane];
+      const uint4 c1 = reinterpret_cast<const uint4*>(sm.bcnt)[2 * lane + 1];
+      const uint32_t sum = c0.x + c0.y + c0.z + c0.w + c1.x + c1.y + c1.z + c1.w;
       uint32_t inc = sum;
 #pragma unroll
       for (int d = 1; d < 32; d <<= 1) {
         const uint32_t t = __shfl_up_sync(0xffffffffu, inc, d);
         if (lane >= d) inc += t;
       }
-      const uint32_t excl = inc - sum;
-#pragma unroll
-      for (int q = 0; q < PER; ++q) {
-        const uint32_t idx = (uint32_t)lane * per + (uint32_t)q;
-        if ((uint32_t)q < per && idx < nb) {
-          sm.bstart[idx] = excl + loc[q];
-          sm.bcnt[idx] = excl + loc[q];
-        }
-      }
-      if (lane == 0) sm.bstart[nb] = m;
+      uint4 s0, s1;
+      s0.x = inc - sum;
+      s0.y = s0.x + c0.x;
+      s0.z = s0.y + c0.y;
+      s0.w = s0.z + c0.z;
+      s1.x = s0.w + c0.w;
+      s1.y = s1.x + c1.x;
+      s1.z = s1.y + c1.y;
+      s1.w = s1.z + c1.z;
+      reinterpret_cast<uint4*>(sm.bstart)[2 * lane] = s0;
+      reinterpret_cast<uint4*>(sm.bstart)[2 * lane + 1] = s1;
+      reinterpret_cast<uint4*>(sm.bcnt)[2 * lane] = s0;
+      reinterpret_cast<uint4*>(sm.bcnt)[2 * lane + 1] = s1;
+      if (lane == 31) sm.bstart[C::NB_MAX] = inc;  // = m
     }
     cbar();
-    GQS_SPLIT_STAMP(11)
+    if ((uint32_t)tid < nb) {  // enter bucket tid in the list of its class
+      const uint32_t c = sm.bstart[tid + 1] - sm.bstart[tid];
+      if (c) {
+        const uint32_t k = c > (uint32_t)C::TINY ? 6u : 32u - (uint32_t)__clz((c - 1u) / (uint32_t)C::R);
+        sm.cls_list[k][atomicAdd(&sm.cls_cnt[k], 1u)] = (uint8_t)tid;
+      }
+    }
     uint32_t j0 = tid;
     for (; j0 + (KU - 1u) * (uint32_t)C::NC < m; j0 += KU * (uint32_t)C::NC) {
       uint32_t pos[KU];
@@ -1434,13 +1505,33 @@ struct Persistent {
       if (GQS_OK(pos < m, a.q, 0xB00Bull)) sm.tileB[pos] = A[i];
     }
     cbar();
-    GQS_SPLIT_STAMP(12)
+    // Tasks in the order class 6, 5, ..., 0; warp w takes tasks w, w + NCW, ...
     uint32_t fin = 0;
-    // warp w takes buckets w, w + NCW, w + 2 NCW, ...
-    for (uint32_t b = (uint32_t)warp; b < nb; b += (uint32_t)C::NCW)
-      fin += place_child(a, sm, A, sm.bstart[b], sm.bstart[b + 1], 1u, lp);
-    GQS_SPLIT_STAMP(13)
-#undef GQS_SPLIT_STAMP
+    uint32_t t = (uint32_t)warp;
+#pragma unroll 1
+    for (int k = 6; k >= 0; --k) {
+      const uint32_t nk = sm.cls_cnt[k];
+      const uint32_t per = k == 6 ? 1u : 32u >> k;
+      const uint32_t ntk = (nk + per - 1u) >> (k == 6 ? 0 : 5 - k);
+      for (; t < ntk; t += (uint32_t)C::NCW) {
+        const uint8_t* list = sm.cls_list[k] + t * per;
+        const uint32_t cnt = min(per, nk - t * per);
+        switch (k) {
+          case 6: {
+            const uint32_t b = list[0];
+            fin += place_child(a, sm, A, sm.bstart[b], sm.bstart[b + 1], 1u, lp);  // a slice-partitioned segment
+            break;
+          }
+          case 5: fin += bucket_networks<32>(sm, A, list, cnt); break;
+          case 4: fin += bucket_networks<16>(sm, A, list, cnt); break;
+          case 3: fin += bucket_networks<8>(sm, A, list, cnt); break;
+          case 2: fin += bucket_networks<4>(sm, A, list, cnt); break;
+          case 1: fin += bucket_networks<2>(sm, A, list, cnt); break;
+          default: fin += bucket_networks<1>(sm, A, list, cnt); break;
+        }
+      }
+      t -= ntk;  // the next class's tasks continue the round robin
+    }
     return fin;
   }
 
@@ -1538,7 +1629,7 @@ struct Persistent {
     unsigned long long st_part = 0, st_local = 0, st_chunks = 0;
     uint32_t st_local_jobs = 0, st_fill_jobs = 0;
     // Leader cycles by item kind (Queue::phase), kept in shared memory by thread 0 alone, so that
-    // no register is held across the loop for them.
+    // no register is held across the loop for them; partition chunks are not timed.
     if (tid == 0) {
       sm.ph[0] = sm.ph[1] = sm.ph[2] = 0ull;
       sm.ph[4] = (unsigned long long)clock64();
@@ -1550,7 +1641,6 @@ struct Persistent {
     cbar();
     for (;;) {
       if (!sm.cons_ok) break;
-      if (tid == 0) sm.ph[3] = (unsigned long long)clock64();
       GQS_PROF_T(t_it)
       GQS_PROF_CNT(PF_N_ITEMS, 1)
       const uint32_t s = k % C::STAGES;
@@ -1600,31 +1690,36 @@ struct Persistent {
         GQS_PROF_ADD(PF_C_COUNT, t_it)
         cbar();  // #1: stage s read into registers; the previous scatter is complete
         GQS_PROF_T(t_l)
-        if (tid == 0) {
-          mbar_arrive(&sm.empty[s]);
-          if (have_scat) post_chunk(a, sm, scat_job);
-          uint32_t ls = 0, gs = 0;
-#pragma unroll
-          for (int w = 0; w < C::NCW; ++w) {
-            ls += sm.wlt[par][w];
-            gs += sm.wgt[par][w];
+        // The bookkeeping between the two barriers is split over three threads of different
+        // warps, so that its waits overlap: warp 0 releases the stage, sums the warp counts,
+        // asks the reserver warp for this chunk's output ranges (used one iteration later, when
+        // this chunk is scattered) and waits for the pending chunk's ranges; lane 0 of warp 1
+        // posts the chunk scattered last iteration to the completer; lane 0 of warp 2 waits for
+        // the next stage. Each publishes its verdict before barrier #2.
+        if (warp == 0) {
+          uint32_t ls = lane < C::NCW ? sm.wlt[par][lane] : 0u, gs = lane < C::NCW ? sm.wgt[par][lane] : 0u;
+          ls = __reduce_add_sync(0xffffffffu, ls);
+          gs = __reduce_add_sync(0xffffffffu, gs);
+          if (lane == 0) {
+            mbar_arrive(&sm.empty[s]);
+            const uint32_t e = npart % C::RQ;
+            sm.rq_job[e] = dd.job;
+            sm.rq_ls[e] = ls;
+            sm.rq_gs[e] = gs;
+            sts_release(&sm.rq_tail, npart + 1);
+            GQS_PROF_T(tw)
+            sm.cons_ok = (!have_pend || leader_wait_reservation(a, sm, npart - 1)) ? 1u : 0u;
+            GQS_PROF_ADD(PF_C_WAIT, tw)
           }
-          // Ask the reserver warp for this chunk's output ranges; they are used one iteration
-          // later, when this chunk is scattered.
-          const uint32_t e = npart % C::RQ;
-          sm.rq_job[e] = dd.job;
-          sm.rq_ls[e] = ls;
-          sm.rq_gs[e] = gs;
-          sts_release(&sm.rq_tail, npart + 1);
-          bool ok = !have_pend || leader_wait_reservation(a, sm, npart - 1);
-          GQS_PROF_T(tw)
-          leader_wait_slot(a, sm, k + 1);
-          if (!ok) sm.cons_ok = 0;
-          GQS_PROF_ADD(PF_C_WAIT, tw)
+        } else if (tid == 32) {
+          if (have_scat) post_chunk(a, sm, scat_job);
+        } else if (tid == 64) {
+          sm.slot_ok = mbar_wait(&sm.full[(k + 1) % C::STAGES], ((k + 1) / C::STAGES) & 1u, a.q, a.timeout_ns, 6)
+                           ? 1u : 0u;
         }
         cbar();  // #2: the pending chunk's ranges are reserved; next slot verdict published
         GQS_PROF_ADD(PF_C_LEADER, t_l)
-        if (!sm.cons_ok) break;
+        if (!sm.cons_ok || !sm.slot_ok) break;
         GQS_PROF_T(t_sc)
         have_scat = false;
         if (have_pend) {
@@ -1652,7 +1747,6 @@ struct Persistent {
         ++npart;
         ++k;
         GQS_PROF_ADD(PF_C_PART, t_it)
-        if (tid == 0) sm.ph[0] += (unsigned long long)clock64() - sm.ph[3];
         continue;
       }
 
@@ -1778,7 +1872,6 @@ struct Persistent {
       if (st_chunks) atomicAdd(&a.q->chunks, st_chunks);
       if (st_local_jobs) atomicAdd(&a.q->local_jobs, st_local_jobs);
       if (st_fill_jobs) atomicAdd(&a.q->fill_jobs, st_fill_jobs);
-      atomicAdd(&a.q->phase[0], sm.ph[0]);
       atomicAdd(&a.q->phase[1], sm.ph[1]);
       atomicAdd(&a.q->phase[2], sm.ph[2]);
       atomicAdd(&a.q->phase[3], (unsigned long long)clock64() - sm.ph[4]);

@@ -293,11 +293,11 @@ gqs_status gqs_last_stats(gqs_ctx* ctx, gqs_stats* out);
 int gqs_last_profile(gqs_ctx* ctx, uint64_t* out, size_t n);
 
 /* Where the last sort's persistent kernel spent its time, on the clock of each CTA's consumer
- * leader thread (SM cycles, summed over CTAs): partition chunk iterations (the gqsort_kernel
- * counterpart), on-chip sorts of ranges of at most one tile (the lqsort_kernel counterpart:
- * tile wait, sort, write-out), writes of queued pivot runs, and the whole consumer loop; the
- * remainder of total_cycles is waiting for work and draining the chunk pipeline. Recorded by
- * every build (a few clock reads per work item). */
+ * leader thread (SM cycles, summed over CTAs): on-chip sorts of ranges of at most one tile (the
+ * lqsort_kernel counterpart: tile wait, sort, write-out), writes of queued pivot runs, and the
+ * whole consumer loop; partition_cycles is the rest of the loop: partition chunk iterations (the
+ * gqsort_kernel counterpart), pipeline drains and waits for work (chunks are not timed one by
+ * one, which would put a clock read on every chunk's critical path). Recorded by every build. */
 typedef struct gqs_phases {
   uint64_t partition_cycles;
   uint64_t onchip_cycles;
