@@ -1769,6 +1769,10 @@ struct Persistent {
       }
       have_pend = false;
       have_scat = false;
+      // The pending keys are dead now; giving them a constant lets the compiler reuse their
+      // registers in the on-chip sort and the fills below (otherwise they stay live around the loop).
+#pragma unroll
+      for (int j = 0; j < C::KPT; ++j) pend[j] = B(0);
       GQS_PROF_ADD(PF_C_DRAIN, t_it)
 
       if (dd.kind == ITEM_TERM) break;
