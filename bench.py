@@ -341,43 +341,56 @@ SERVE_TYPES = ("u32", "f32", "f64")
 
 
 class OutPool:
-    """Ring allocator over one pinned host buffer for request outputs (client-side window)."""
+    """First-fit allocator over one pinned host buffer for request outputs (the client-side
+    window: a submit waits while the buffer holds no room). Blocks are freed in any order and
+    merged with free neighbours, so one slow request does not hold back the space behind it.
+    Records how long allocations waited."""
 
     def __init__(self, nbytes):
-        import collections
         import threading
         import torch
         self.buf = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
         self.base = self.buf.data_ptr()
         self.size = nbytes
-        self.head = 0
-        self.live = collections.deque()  # [start, end, done] in allocation order
+        self.free_list = [[0, nbytes]]  # [start, end), sorted by start, never adjacent
         self.cv = threading.Condition()
+        self.wait_s = 0.0
+        self.waits = 0
 
     def alloc(self, nbytes):
         nbytes = (nbytes + 255) // 256 * 256
+        t0 = None
         with self.cv:
             while True:
-                while self.live and self.live[0][2]:
-                    self.live.popleft()
-                if not self.live:
-                    self.head = 0
-                    lo, hi = 0, self.size
-                else:
-                    first = self.live[0][0]
-                    lo, hi = (self.head, self.size) if self.head > first else (self.head, first)
-                    if self.head > first and lo + nbytes > hi:
-                        lo, hi = 0, first  # wrap
-                if lo + nbytes <= hi:
-                    rec = [lo, lo + nbytes, False]
-                    self.live.append(rec)
-                    self.head = lo + nbytes
-                    return rec
+                for blk in self.free_list:
+                    if blk[1] - blk[0] >= nbytes:
+                        lo = blk[0]
+                        blk[0] += nbytes
+                        if blk[0] == blk[1]:
+                            self.free_list.remove(blk)
+                        if t0 is not None:
+                            self.wait_s += time.perf_counter() - t0
+                            self.waits += 1
+                        return [lo, lo + nbytes]
+                if t0 is None:
+                    t0 = time.perf_counter()
                 self.cv.wait()
 
     def free(self, rec):
+        import bisect
+        lo, hi = rec
         with self.cv:
-            rec[2] = True
+            fl = self.free_list
+            k = bisect.bisect_left([b[0] for b in fl], lo)
+            if k > 0 and fl[k - 1][1] == lo:
+                fl[k - 1][1] = hi
+                if k < len(fl) and fl[k][0] == hi:
+                    fl[k - 1][1] = fl[k][1]
+                    del fl[k]
+            elif k < len(fl) and fl[k][0] == hi:
+                fl[k][0] = lo
+            else:
+                fl.insert(k, [lo, hi])
             self.cv.notify_all()
 
 
@@ -434,6 +447,8 @@ def run_serve_arm(gqs_ctypes, templates, stream, per_request, rate, pool, sample
     col.start()
     t0 = srv.now_ns()
     t_wall0 = time.perf_counter()
+    w0, nw0 = pool.wait_s, pool.waits
+    call_s = np.zeros(count)
     for i in range(count):
         if rate:
             delay = arrive[i] - (time.perf_counter() - t_wall0)
@@ -444,9 +459,11 @@ def run_serve_arm(gqs_ctypes, templates, stream, per_request, rate, pool, sample
         rec = pool.alloc(nb)
         recs[i] = rec
         tmpl = templates[t]
+        tc = time.perf_counter()
         with lock:
             rid = srv.submit_raw(t, tmpl.data_ptr() + int(src[i]) * esz[dt[i]], pool.base + rec[0], int(n[i]))
             idx_of[rid] = i
+        call_s[i] = time.perf_counter() - tc
     col.join()
     gc.enable()
     st = srv.stats()
@@ -472,7 +489,13 @@ def run_serve_arm(gqs_ctypes, templates, stream, per_request, rate, pool, sample
         split[t] = {name: {"p50_ms": float(np.percentile(v, 50)), "p99_ms": float(np.percentile(v, 99))}
                     for name, v in parts.items()}
         split[t]["requests"] = int(m.sum())
+    client = {"output_window_waits": pool.waits - nw0, "output_window_wait_s": pool.wait_s - w0,
+              "submit_call_p99_ms": float(np.percentile(call_s, 99) * 1e3),
+              "submit_call_max_ms": float(call_s.max() * 1e3)}
+    srv_ms = (done - sub) / 1e6
     return {"keys_per_s": float(n.sum()) / span, "span_s": span, "lat_ms": lat_ms, "split": split,
+            "server_p50_ms": float(np.percentile(srv_ms, 50)), "server_p99_ms": float(np.percentile(srv_ms, 99)),
+            "client": client,
             "batches": st["batches"], "max_batch_requests": st["max_batch_requests"],
             "arena_peak_gb": st["arena_peak"] / 1e9}, samples
 
@@ -490,7 +513,7 @@ def run_serve(args, gqs_ctypes):
         v = buf.numpy().view(gqs_ctypes.NP_DTYPES[t])
         gqs_ctypes.generate(t, SERVE_DIST[t], SEED + 7 * k, v.size, out=v)
         templates[t] = buf
-    pool = OutPool(3 << 30)
+    pool = OutPool(6 << 30)
     # warm-up: a short stream through both modes (graph capture, pool growth)
     warm = serve_stream(64, SEED + 1)
     run_serve_arm(gqs_ctypes, templates, warm, False, None, pool)
@@ -517,6 +540,7 @@ def run_serve(args, gqs_ctypes):
     def lat(r):
         return {"p50_ms": float(np.percentile(r["lat_ms"], 50)), "p99_ms": float(np.percentile(r["lat_ms"], 99)),
                 "gkeys_s": r["keys_per_s"] / 1e9, "span_s": r["span_s"], "batches": r["batches"],
+                "server_p50_ms": r["server_p50_ms"], "server_p99_ms": r["server_p99_ms"], "client": r["client"],
                 "split_by_type": r["split"]}
 
     total_keys = int(n.sum())

@@ -17,6 +17,7 @@
 #include "gqs_device.cuh"
 #include "gqs_host.h"
 #include "gqs_launch.h"
+#include "gqs_tuning.h"
 
 namespace gqs {
 
@@ -52,6 +53,28 @@ cudaError_t launch_sort(int dtype, const LaunchParams& p) {
     case DT_U64: return launch_u64(p);
     default: return launch_f64(p);
   }
+}
+
+// The tuning table's variant for n keys of `dtype` on a GPU of `sms` SMs: the rows of the
+// nearest SM count measured, then the nearest size class (ceil(log2 n)); 0 without a row.
+int tuned_variant(int dtype, size_t n, int sms) {
+  int lg = 0;
+  while (lg < 63 && (1ull << lg) < (unsigned long long)n) ++lg;
+  int best_sms = -1, v = 0, best = 1 << 30;
+  for (const TuneRow& r : kTuneRows) {
+    if (r.dtype != dtype) continue;
+    const int d = r.sms > sms ? r.sms - sms : sms - r.sms;
+    if (best_sms < 0 || d < (best_sms > sms ? best_sms - sms : sms - best_sms)) best_sms = r.sms;
+  }
+  for (const TuneRow& r : kTuneRows) {
+    if (r.dtype != dtype || r.sms != best_sms) continue;
+    const int d = r.log2n > lg ? r.log2n - lg : lg - r.log2n;
+    if (d < best) {
+      best = d;
+      v = r.variant;
+    }
+  }
+  return v >= 0 && v < variant_count(dtype) ? v : 0;
 }
 
 }  // namespace gqs
@@ -118,6 +141,7 @@ struct gqs_ctx {
   unsigned long long last_lvl_start = 0;
 #endif
   int variant[4] = {0, 0, 0, 0};  // per key type, and the internal packed pairs
+  bool auto_variant[4] = {true, true, true, true};  // pick per call from the tuning table
   int blocks_per_sm[4][kMaxVariants] = {};
 };
 
@@ -183,7 +207,7 @@ gqs_status enqueue_locked(gqs_ctx* c, int dtype, void* d, void* dn, size_t n, co
   if (!d || (reinterpret_cast<uintptr_t>(d) % es) != 0) return GQS_ERR_INVALID;
   if (dn && (reinterpret_cast<uintptr_t>(dn) % es) != 0) return GQS_ERR_INVALID;
   if (n >= (1ull << 40) || nseg >= (1ull << 31)) return GQS_ERR_INVALID;
-  const int v = c->variant[dtype];
+  const int v = c->auto_variant[dtype] ? gqs::tuned_variant(dtype, n, c->num_sms) : c->variant[dtype];
   const gqs::VariantInfo vi = gqs::variant_info(dtype, v);
   const size_t cap = job_capacity(vi, n, nseg);
   const size_t ring = ticket_ring(vi, n, nseg);
@@ -596,6 +620,7 @@ gqs_status gqs_create(gqs_ctx** out, int device, const gqs_config* cfg) {
     if (cudaMallocHost(&c->q_host, sizeof(gqs::Queue)) != cudaSuccess) { st = GQS_ERR_NOMEM; break; }
     for (int t = 0; t < 4; ++t) {
       int v = c->cfg.variant;
+      c->auto_variant[t] = v < 0;
       if (v < 0 || v >= gqs::variant_count(t)) v = 0;
       c->variant[t] = v;
     }
@@ -643,7 +668,7 @@ gqs_status gqs_reserve(gqs_ctx* c, int dtype, size_t n, size_t nseg, int with_bu
   std::lock_guard<std::mutex> lk(c->mu);
   DeviceGuard dg(c->device);
   (void)wait_pending_locked(c);
-  const int v = c->variant[dtype];
+  const int v = c->auto_variant[dtype] ? gqs::tuned_variant(dtype, n, c->num_sms) : c->variant[dtype];
   const gqs::VariantInfo vi = gqs::variant_info(dtype, v);
   if (!c->blocks_per_sm[dtype][v]) {
     c->blocks_per_sm[dtype][v] = gqs::variant_prepare(dtype, v);
@@ -896,12 +921,13 @@ gqs_status gqs_set_variant(gqs_ctx* c, int dtype, int v) {
   if (!c || dtype < 0 || dtype > 2 || v < 0 || v >= gqs::variant_count(dtype)) return GQS_ERR_INVALID;
   std::lock_guard<std::mutex> lk(c->mu);
   c->variant[dtype] = v;
+  c->auto_variant[dtype] = false;
   return GQS_OK;
 }
 
 int gqs_get_variant(gqs_ctx* c, int dtype) {
   if (!c || dtype < 0 || dtype > 2) return -1;
-  return c->variant[dtype];
+  return c->auto_variant[dtype] ? -1 : c->variant[dtype];
 }
 
 const char* gqs_strerror(gqs_status s) {

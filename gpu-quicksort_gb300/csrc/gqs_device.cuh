@@ -272,6 +272,7 @@ struct alignas(128) Smem {
   // the buckets of each network class (appended in any order) and their numbers
   uint8_t cls_list[C::NCLASS][C::NB_MAX];
   uint32_t cls_cnt[8];
+  uint32_t task_next;  // the next bucket task to take
   uint8_t lb[C::TILE];
 };
 
@@ -1367,7 +1368,7 @@ struct Persistent {
   //  4. Every key is scattered into tileB at its bucket's place; meanwhile each bucket is entered
   //     in the list of its class: class c <= 5 is sorted by a group of 2^c lanes holding R keys
   //     each (2^c * R keys at most), class 6 holds the buckets longer than TINY.
-  //  5. Tasks, dealt round robin to the warps largest class first: a class-6 bucket becomes a
+  //  5. Tasks, largest class first, each taken by the next free warp: a class-6 bucket becomes a
   //     slice-partitioned segment; a class-c task sorts 32 >> c buckets of that class at once.
   // The buckets are disjoint ranges in final order. (Inlined: as a called function its register
   // demand made the kernel keep partition-loop values in local memory.)
@@ -1381,6 +1382,7 @@ struct Persistent {
     }
     for (uint32_t i = tid; i < (uint32_t)C::NB_MAX; i += C::NC) sm.bcnt[i] = 0u;
     if (tid < 8) sm.cls_cnt[tid] = 0u;
+    if (tid == 0) sm.task_next = 0u;
     constexpr int RS = C::SPLIT_SAMPLES / 32;  // samples per lane
     constexpr int RUN = C::SPLIT_RUN;
     constexpr int NRUN = C::SPLIT_SAMPLES / RUN;
@@ -1505,32 +1507,38 @@ struct Persistent {
       if (GQS_OK(pos < m, a.q, 0xB00Bull)) sm.tileB[pos] = A[i];
     }
     cbar();
-    // Tasks in the order class 6, 5, ..., 0; warp w takes tasks w, w + NCW, ...
+    // Tasks in the order class 6, 5, ..., 0 (largest networks first); each warp takes the next
+    // task from a shared counter whenever it is free, so the long tasks spread first and the
+    // short ones fill the gaps.
     uint32_t fin = 0;
-    uint32_t t = (uint32_t)warp;
-#pragma unroll 1
-    for (int k = 6; k >= 0; --k) {
-      const uint32_t nk = sm.cls_cnt[k];
-      const uint32_t per = k == 6 ? 1u : 32u >> k;
-      const uint32_t ntk = (nk + per - 1u) >> (k == 6 ? 0 : 5 - k);
-      for (; t < ntk; t += (uint32_t)C::NCW) {
-        const uint8_t* list = sm.cls_list[k] + t * per;
-        const uint32_t cnt = min(per, nk - t * per);
-        switch (k) {
-          case 6: {
-            const uint32_t b = list[0];
-            fin += place_child(a, sm, A, sm.bstart[b], sm.bstart[b + 1], 1u, lp);  // a slice-partitioned segment
-            break;
-          }
-          case 5: fin += bucket_networks<32>(sm, A, list, cnt); break;
-          case 4: fin += bucket_networks<16>(sm, A, list, cnt); break;
-          case 3: fin += bucket_networks<8>(sm, A, list, cnt); break;
-          case 2: fin += bucket_networks<4>(sm, A, list, cnt); break;
-          case 1: fin += bucket_networks<2>(sm, A, list, cnt); break;
-          default: fin += bucket_networks<1>(sm, A, list, cnt); break;
-        }
+    for (;;) {
+      uint32_t t = 0;
+      if (lane == 0) t = atomicAdd(&sm.task_next, 1u);
+      t = __shfl_sync(0xffffffffu, t, 0);
+      int k = 6;
+      uint32_t per = 1u, ntk = sm.cls_cnt[6];
+      while (t >= ntk && k > 0) {  // skip whole classes: t becomes the index within class k
+        t -= ntk;
+        --k;
+        per = 32u >> k;
+        ntk = (sm.cls_cnt[k] + per - 1u) >> (5 - k);
       }
-      t -= ntk;  // the next class's tasks continue the round robin
+      if (t >= ntk) break;  // past the last task of class 0
+      const uint8_t* list = sm.cls_list[k] + t * per;
+      const uint32_t cnt = min(per, sm.cls_cnt[k] - t * per);
+      switch (k) {
+        case 6: {
+          const uint32_t b = list[0];
+          fin += place_child(a, sm, A, sm.bstart[b], sm.bstart[b + 1], 1u, lp);  // a slice-partitioned segment
+          break;
+        }
+        case 5: fin += bucket_networks<32>(sm, A, list, cnt); break;
+        case 4: fin += bucket_networks<16>(sm, A, list, cnt); break;
+        case 3: fin += bucket_networks<8>(sm, A, list, cnt); break;
+        case 2: fin += bucket_networks<4>(sm, A, list, cnt); break;
+        case 1: fin += bucket_networks<2>(sm, A, list, cnt); break;
+        default: fin += bucket_networks<1>(sm, A, list, cnt); break;
+      }
     }
     return fin;
   }

@@ -49,7 +49,7 @@ typedef enum gqs_status {
 typedef enum gqs_dtype { GQS_U32 = 0, GQS_F32 = 1, GQS_F64 = 2 } gqs_dtype;
 
 typedef struct gqs_config {
-  int32_t variant;     /* -1: the context's tuned choice per key type; else a variant index */
+  int32_t variant;     /* -1: per sort, the tuned variant for its key type and size; else fixed */
   uint32_t timeout_ms; /* device-side no-progress limit for bounded waits; 0 means 4000 */
   uint32_t sync;       /* 1 (default): *_dev calls wait for the stream and return the device status */
   uint32_t timing;     /* 1: time the persistent kernel with CUDA events (gqs_stats.kernel_ms) */
@@ -327,7 +327,13 @@ typedef struct gqs_level {
  * (libgqs_prof.so) records them; the product library returns 0. */
 int gqs_last_levels(gqs_ctx* ctx, gqs_level* out, int max);
 
-/* Kernel variants available for a key type, and the one the context currently uses. */
+/* Kernel variants available for a key type (gqs_variant_describe: tile, chunk, CTA size). A
+ * context created with cfg.variant = -1 picks, for every sort, the variant a tuning run on the
+ * GPU found fastest for that key type and size class (ceil(log2 n)) on a GPU with the nearest
+ * SM count: the counterpart of the reference's size-dependent launch parameters (optp,
+ * GPU-Quicksort_Full_SYCL/QuicksortMain.cpp:831-833). gqs_set_variant fixes one variant for a key
+ * type instead; gqs_get_variant returns it, or -1 while the context picks per sort (the variant a
+ * sort ran with is in gqs_stats.variant). */
 int gqs_variant_count(int dtype);
 gqs_status gqs_variant_describe(int dtype, int variant, gqs_variant_desc* out);
 gqs_status gqs_set_variant(gqs_ctx* ctx, int dtype, int variant);

@@ -353,3 +353,52 @@ def test_random_sizes_every_variant(dtype):
                 assert ctx.stats()["status"] == 0
         finally:
             ctx.close()
+
+
+# ---------------------------------------------------------------------------
+# size-aware variant choice (the counterpart of the reference's optp size rule)
+
+def _tuning_rows():
+    import re
+    text = open(os.path.join(os.path.dirname(os.path.dirname(__file__)), "gpu-quicksort_gb300", "csrc",
+                             "gqs_tuning.h")).read()
+    body = text[text.index("kTuneRows[] = {"):]
+    return [tuple(int(x) for x in m) for m in re.findall(r"\{(\d+), (\d+), (\d+), (\d+)\}", body)]
+
+
+def _expected_variant(rows, dtype_id, n, sms):
+    lg = max(0, int(np.ceil(np.log2(max(n, 1)))))
+    cand = [r for r in rows if r[1] == dtype_id]
+    near = min(cand, key=lambda r: abs(r[0] - sms))[0]
+    return min((r for r in cand if r[0] == near), key=lambda r: abs(r[2] - lg))[3]
+
+
+def test_variant_follows_size(gpu_ctx):
+    """A context created with variant -1 runs each sort with the variant the tuning table names
+    for its key type and size class; the table picks different variants at different sizes, and
+    every result stays bit-exact against std::sort. A fixed variant is kept at every size."""
+    torch = _torch()
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    rows = _tuning_rows()
+    sizes = [1 << k for k in range(10, 25)] + [3000, 100_003, 1_500_007]
+    seen = set()
+    for dtype, did in (("u32", 0), ("f32", 1), ("f64", 2)):
+        for n in sizes:
+            a = gqs_ctypes.generate(dtype, "uniform" if dtype != "f32" else "gaussian", 900 + n, n)
+            b = a.copy()
+            gpu_ctx.sort(b)
+            assert np.array_equal(b.view(np.uint8), oracle_sorted(a).view(np.uint8)), (dtype, n)
+            st = gpu_ctx.stats()
+            want = _expected_variant(rows, did, n if n < (1 << 24) else n // 4, sms)
+            assert st["variant"] == want, (dtype, n, st["variant"], want)
+            seen.add((did, st["variant"]))
+    assert len({v for d, v in seen if d == 0}) > 1, "the table names one variant for every u32 size"
+    assert gpu_ctx.get_variant("u32") == -1
+    ctx = gqs_ctypes.Context(variant=2)
+    try:
+        for n in (1 << 12, 1 << 18, 1 << 21):
+            a = gqs_ctypes.generate("u32", "uniform", 5, n)
+            ctx.sort(a)
+            assert ctx.stats()["variant"] == 2 and ctx.get_variant("u32") == 2
+    finally:
+        ctx.close()
