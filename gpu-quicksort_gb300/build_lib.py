@@ -26,7 +26,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
               "--expt-relaxed-constexpr", "-I" + CSRC, "-I" + INCLUDE]
 CU_SOURCES = ["gqs_sort_dispatch.cu", "gqs_capi.cu", "gqs_noalloc.cu", "gqs_batch.cu", "gqs_serve.cu",
-              "gqs_merge.cu"]
+              "gqs_merge.cu", "gqs_split.cu"]
 VARIANT_TU = "gqs_variant_tu.cu"  # compiled once per (key type, variant index)
 
 LIB = os.path.join(HERE, "libgqs.so")

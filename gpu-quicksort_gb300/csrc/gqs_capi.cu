@@ -140,6 +140,9 @@ struct gqs_ctx {
   unsigned long long last_lvl[gqs::kLevels][6] = {};  // per-level rows of the last sort
   unsigned long long last_lvl_start = 0;
 #endif
+  void* split_buf = nullptr;  // scratch of the top split of small sorts (gqs_split.cu)
+  size_t split_bytes = 0;
+  bool top_split = true;
   int variant[4] = {0, 0, 0, 0};  // per key type, and the internal packed pairs
   bool auto_variant[4] = {true, true, true, true};  // pick per call from the tuning table
   int blocks_per_sm[4][kMaxVariants] = {};
@@ -209,8 +212,12 @@ gqs_status enqueue_locked(gqs_ctx* c, int dtype, void* d, void* dn, size_t n, co
   if (n >= (1ull << 40) || nseg >= (1ull << 31)) return GQS_ERR_INVALID;
   const int v = c->auto_variant[dtype] ? gqs::tuned_variant(dtype, n, c->num_sms) : c->variant[dtype];
   const gqs::VariantInfo vi = gqs::variant_info(dtype, v);
-  const size_t cap = job_capacity(vi, n, nseg);
-  const size_t ring = ticket_ring(vi, n, nseg);
+  // Small plain sorts start with a multi-way split whose buckets become the segments.
+  gqs::SplitPlan plan{};
+  const bool split = !offsets && !check_n && c->top_split && gqs::split_plan(dtype, n, vi.tile, c->num_sms, &plan);
+  const size_t segs = split ? plan.k : nseg;
+  const size_t cap = job_capacity(vi, n, segs);
+  const size_t ring = ticket_ring(vi, n, segs);
   if (cap >= (1ull << 32) || ring > (1ull << 31)) return GQS_ERR_INVALID;
   if (!c->blocks_per_sm[dtype][v]) {
     c->blocks_per_sm[dtype][v] = gqs::variant_prepare(dtype, v);
@@ -220,7 +227,8 @@ gqs_status enqueue_locked(gqs_ctx* c, int dtype, void* d, void* dn, size_t n, co
   const bool need_jobs = c->job_cap < cap;
   const bool need_dn = !dn && c->pool_dn_bytes < n * es;
   const bool need_ring = c->tmap_len < ring;
-  if (need_jobs || need_dn || need_ring) {
+  const bool need_split = split && c->split_bytes < gqs::split_scratch_bytes(plan);
+  if (need_jobs || need_dn || need_ring || need_split) {
     st = wait_pending_locked(c);
     if (st != GQS_OK && st != GQS_ERR_TIMEOUT && st != GQS_ERR_CAPACITY && st != GQS_ERR_INTERNAL) return st;
     size_t bytes = 0;
@@ -242,6 +250,10 @@ gqs_status enqueue_locked(gqs_ctx* c, int dtype, void* d, void* dn, size_t n, co
     }
     if (need_dn) {
       st = grow(&c->pool_dn, &c->pool_dn_bytes, n * es);
+      if (st != GQS_OK) return st;
+    }
+    if (need_split) {
+      st = grow(&c->split_buf, &c->split_bytes, gqs::split_scratch_bytes(plan));
       if (st != GQS_OK) return st;
     }
   }
@@ -273,6 +285,16 @@ gqs_status enqueue_locked(gqs_ctx* c, int dtype, void* d, void* dn, size_t n, co
   p.ev_begin = c->cfg.timing ? c->ev_begin : nullptr;
   p.ev_end = c->cfg.timing ? c->ev_end : nullptr;
   p.check_n = check_n;
+  if (split) {  // the timed interval starts with the split
+    if (p.ev_begin && (e = cudaEventRecord(p.ev_begin, stream)) != cudaSuccess) return cuda_status(e);
+    p.ev_begin = nullptr;
+    unsigned long long* table = nullptr;
+    e = gqs::split_launch(dtype, plan, d, dn, n, c->split_buf, &table, c->q, stream);
+    if (e != cudaSuccess) return cuda_status(e);
+    p.offsets = table;
+    p.nseg = plan.k;
+    p.from_dn = 1;
+  }
   e = gqs::launch_sort(dtype, p);
   if (e != cudaSuccess) return cuda_status(e);
   e = cudaEventRecord(c->ev_done, stream);
@@ -659,6 +681,7 @@ void gqs_destroy(gqs_ctx* c) {
       if (ev) cudaEventDestroy(ev);
     if (c->q_acc) cudaFree(c->q_acc);
     if (c->merge_splits) cudaFree(c->merge_splits);
+    if (c->split_buf) cudaFree(c->split_buf);
   }
   delete c;
 }
@@ -675,6 +698,15 @@ gqs_status gqs_reserve(gqs_ctx* c, int dtype, size_t n, size_t nseg, int with_bu
     if (!c->blocks_per_sm[dtype][v]) return GQS_ERR_NO_DEVICE;
   }
   if (n >= (1ull << 40) || nseg >= (1ull << 31)) return GQS_ERR_INVALID;
+  // a plain sort of this size may start with the top split: its buckets are segments, and it
+  // has scratch of its own
+  gqs::SplitPlan plan{};
+  const bool split = nseg <= 1 && c->top_split && gqs::split_plan(dtype, n, vi.tile, c->num_sms, &plan);
+  if (split) {
+    nseg = plan.k;
+    gqs_status st = grow(&c->split_buf, &c->split_bytes, gqs::split_scratch_bytes(plan));
+    if (st != GQS_OK) return st;
+  }
   const size_t cap = job_capacity(vi, n, nseg ? nseg : 1);
   if (cap >= (1ull << 32) || ticket_ring(vi, n, nseg ? nseg : 1) > (1ull << 31)) return GQS_ERR_INVALID;
   if (c->job_cap < cap) {

@@ -656,11 +656,12 @@ __device__ unsigned long long dispatch_range(const SortArgs<typename C::T>& a, u
 
 // Segment i is [offsets[i], offsets[i+1]) or, with `pairs`, [offsets[2i], offsets[2i+1]) (the
 // segments then need not be adjacent); without offsets, the one segment [0, n). Every segment
-// must lie in [0, n).
+// must lie in [0, n). The keys are in d, or with `from_dn` in dn (the buckets of a top split);
+// either way the sorted keys end in d.
 template <class C>
 __global__ void __launch_bounds__(256) seed_kernel(SortArgs<typename C::T> a, const unsigned long long* offsets,
                                                    const unsigned long long* nseg_dev, uint32_t nseg,
-                                                   unsigned long long n, uint32_t pairs) {
+                                                   unsigned long long n, uint32_t pairs, uint32_t from_dn) {
   const uint32_t seg = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (nseg_dev) {  // a replayable launch: the count is data, at most the launch's capacity
@@ -681,7 +682,8 @@ __global__ void __launch_bounds__(256) seed_kernel(SortArgs<typename C::T> a, co
   if (e == s) return;
   if (lane == 0) atomicAdd(&a.q->total, e - s);
   unsigned long long tiny = 0;
-  const unsigned long long placed = dispatch_range<C>(a, 1u, s, e, 0u, tiny);
+  // the buckets of a top split are its children: depth 1
+  const unsigned long long placed = dispatch_range<C>(a, from_dn ? 0u : 1u, s, e, from_dn ? 1u : 0u, tiny);
   if (lane == 0) {
     if (placed) atomicAdd(&a.q->done, placed);
     if (tiny) atomicAdd(&a.q->tiny_keys, tiny);

@@ -39,6 +39,7 @@ struct LaunchParams {
   uint32_t nseg;                      // segments (with nseg_dev: the most the launch may see)
   const unsigned long long* nseg_dev; // optional: segment count read on the device (replayable graphs)
   uint32_t pairs;                     // 1: offsets holds (start, end) per segment, 2 * nseg entries
+  uint32_t from_dn;                   // 1: the segments' keys are in dn (buckets of a top split)
   int variant;
   int grid;
   cudaStream_t stream;
@@ -78,5 +79,20 @@ cudaError_t merge_tiles(int dtype, const void* a, size_t na, const void* b, size
                         const unsigned long long* splits, size_t t0, size_t t1, cudaStream_t s);
 cudaError_t merge_runs(int dtype, const void* a, size_t na, const void* b, size_t nb, void* out,
                        unsigned long long* splits, cudaStream_t s);
+
+// Top split of a plain sort of n keys (defined in gqs_split.cu): picks K - 1 splitters from
+// sorted samples of d, counts every key's bucket per CTA, scans the counts into bucket offsets
+// (segs, K + 1 entries) and scatters the keys into dn bucket by bucket. The buckets are then
+// sorted as segments whose keys are in dn. `scratch` holds split_scratch_bytes(dtype, n) bytes.
+struct SplitPlan {
+  uint32_t k;      // buckets (a power of two, 2 .. 1024)
+  uint32_t lg;     // log2 k
+  uint32_t ctas;   // CTAs of the count and scatter kernels
+  uint32_t samples;
+};
+bool split_plan(int dtype, size_t n, int tile, int sms, SplitPlan* plan);
+size_t split_scratch_bytes(const SplitPlan& plan);
+cudaError_t split_launch(int dtype, const SplitPlan& plan, const void* d, void* dn, size_t n, void* scratch,
+                         unsigned long long** segs, Queue* q, cudaStream_t s);
 
 }  // namespace gqs

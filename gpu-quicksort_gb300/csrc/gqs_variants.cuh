@@ -45,7 +45,7 @@ struct VariantOps {
     a.n = p.check_n ? p.check_n : p.n;
     const uint32_t nseg = p.offsets ? p.nseg : 1u;
     const uint32_t seed_blocks = (nseg + 7u) / 8u;  // 8 warps per 256-thread block, one per segment
-    seed_kernel<C><<<seed_blocks, 256, 0, p.stream>>>(a, p.offsets, p.nseg_dev, nseg, p.n, p.pairs);
+    seed_kernel<C><<<seed_blocks, 256, 0, p.stream>>>(a, p.offsets, p.nseg_dev, nseg, p.n, p.pairs, p.from_dn);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     if (p.ev_begin) cudaEventRecord(p.ev_begin, p.stream);

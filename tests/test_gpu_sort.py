@@ -402,3 +402,38 @@ def test_variant_follows_size(gpu_ctx):
             assert ctx.stats()["variant"] == 2 and ctx.get_variant("u32") == 2
     finally:
         ctx.close()
+
+
+# ---------------------------------------------------------------------------
+# the top split of small plain sorts (2^15 .. 2^21 keys)
+
+@pytest.mark.parametrize("dtype", ["u32", "f32", "f64"])
+def test_top_split_range(gpu_ctx, dtype):
+    """Plain sorts of 2^15 .. 2^21 keys start with a multi-way split whose buckets are then sorted
+    as segments: sizes at both ends of that range and just outside it, every distribution
+    (all-equal keys put the whole array in one bucket), through both entry points, bit-exact
+    against std::sort; the split is counted as one partition pass."""
+    torch = _torch()
+    for n in ((1 << 15) - 1, 1 << 15, 40_000, 300_007, 1 << 21, (1 << 21) + 1):
+        for dist in (DISTS[dtype] if n <= 300_007 else ("uniform", "distinct16", "allequal")):
+            a = gqs_ctypes.generate(dtype, dist, 4400 + n, n)
+            ref = oracle_sorted(a)
+            b = a.copy()
+            gpu_ctx.sort(b)
+            assert np.array_equal(b.view(np.uint8), ref.view(np.uint8)), (dtype, dist, n)
+            st = gpu_ctx.stats()
+            assert st["status"] == 0 and st["keys"] == n
+            if (1 << 15) <= n <= (1 << 21):
+                assert st["part_keys"] >= n, "the split pass is counted"
+        t = torch.from_numpy(a.view(np.int32) if dtype == "u32" else a).cuda()
+        assert gpu_ctx.sort_dev(dtype, t.data_ptr(), None, n, torch.cuda.current_stream().cuda_stream) == 0
+        out = t.cpu().numpy()
+        assert np.array_equal(out.view(np.uint8), ref.view(np.uint8)), (dtype, "dev", n)
+
+
+def test_top_split_pairs(gpu_ctx):
+    """Key-value sorts in the split range: stable argsort equal to numpy's."""
+    for n in (1 << 15, 123_457, 1 << 20):
+        keys = gqs_ctypes.generate("u32", "distinct16", 77 + n, n)
+        idx = gpu_ctx.argsort(keys)
+        assert np.array_equal(idx, np.argsort(keys, kind="stable").astype(np.uint32))
