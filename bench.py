@@ -1081,9 +1081,23 @@ def main():
             runner.ctx.sort(wv)
             times.append(time.perf_counter() - t0)
         tsum = max_over_ranks(sum(times), dist)
+        # this machine's host link, for reading the end-to-end number: one pinned copy each way
+        nb = n * esize
+        link = {}
+        for name, dst, src in (("h2d_gbs", runner.d[:nb], work), ("d2h_gbs", work, runner.d[:nb])):
+            e0, e1 = _t.cuda.Event(enable_timing=True), _t.cuda.Event(enable_timing=True)
+            dst.copy_(src, non_blocking=True)
+            e0.record()
+            dst.copy_(src, non_blocking=True)
+            e1.record()
+            _t.cuda.synchronize()
+            link[name] = nb / (e0.elapsed_time(e1) / 1e3) / 1e9
         e2e = {"value": n * world * args.steps / tsum / 1e9, "unit": "Gkeys/s",
                "h2d_bytes_per_step": n * esize, "d2h_bytes_per_step": n * esize,
                "ms_per_step": 1e3 * tsum / args.steps, "api": "gqs_sort_" + args.dtype + " (host pointers, pinned)",
+               "median_ms_per_step": 1e3 * float(np.median(times)), "max_ms_per_step": 1e3 * max(times),
+               "link": link,
+               "copies_alone_ms": 1e3 * (nb / (link["h2d_gbs"] * 1e9) + nb / (link["d2h_gbs"] * 1e9)),
                "check": golden_check(golden_case(args.dtype, args.dist, n, SEED + rank), r["hv"], wv)}
         del work
 
