@@ -215,7 +215,6 @@ struct Cfg {
   static constexpr int NB_MAX = 256;
   static constexpr int SPLIT_MIN = 8 * TINY;
   static constexpr int SPLIT_SAMPLES = 256;
-  static constexpr int SPLIT_RUN = 32;                 // samples are sorted as runs of 32
   static constexpr int BUCKET = TINY / GQS_BUCKET_DIV;  // mean bucket size the split aims for
   static constexpr int NCLASS = 7;                     // bucket classes (network sizes), see sample_split
   static_assert(CHUNK % NC == 0, "chunk must be a multiple of the consumer threads");
@@ -223,8 +222,8 @@ struct Cfg {
   static_assert((CHUNK * sizeof(B)) % 16 == 0, "chunk must be a multiple of 16 bytes");
   static_assert(TILE > TINY, "tile must exceed the register sort");
   static_assert(NB_MAX <= 256 && NB_MAX >= 32, "bucket labels are bytes; the scan takes 32..256 buckets");
-  static_assert(SPLIT_SAMPLES == 256 && NB_MAX == 256, "8 samples and 8 bucket counts per lane of one warp");
-  static_assert(SPLIT_RUN == 32 && NC >= SPLIT_SAMPLES, "runs of 32 samples, one thread per sample");
+  static_assert(NB_MAX == 256, "8 bucket counts per lane of one warp in the scan");
+  static_assert(SPLIT_SAMPLES >= NB_MAX && NC >= SPLIT_SAMPLES, "one pivot per bucket; one thread per sample");
 };
 
 // A segment of the on-chip tile being partitioned slice by slice (shared memory).
@@ -1359,11 +1358,10 @@ struct Persistent {
   // First level of the on-chip sort for tiles of SPLIT_MIN keys or more: one multi-pivot
   // partition of the whole tile into nb buckets (nb a power of two, buckets of about BUCKET keys),
   // then every bucket sorted in registers. Whole CTA; returns the keys this warp finalised.
-  //  1. Pivots. Warp 0 sorts SPLIT_SAMPLES evenly spaced keys as runs of 32 (groups of 4 lanes,
-  //     8 samples each); every sample then finds its rank among all of them, by binary searches
-  //     in the other runs, and the sample of rank (q + 1) * (SPLIT_SAMPLES / nb) - 1 becomes
-  //     pivot q. The pivots are stored as an implicit search tree in breadth-first order (node i
-  //     has children 2i and 2i + 1), so the lanes of a warp reading one level hit distinct banks.
+  //  1. Pivots. SPLIT_SAMPLES evenly spaced keys, each ranked by one thread that compares it with
+  //     all of them; the sample of rank (q + 1) * (SPLIT_SAMPLES / nb) - 1 becomes pivot q. The
+  //     pivots are stored as an implicit search tree in breadth-first order (node i has children
+  //     2i and 2i + 1), so the lanes of a warp reading one level hit distinct banks.
   //  2. Every consumer thread labels its keys with their bucket (bucket b holds
   //     pivot[b-1] < key <= pivot[b]) and counts them.
   //  3. Warp 0 scans the counts (16-byte loads and stores): bucket starts, and scatter cursors.
@@ -1385,43 +1383,27 @@ struct Persistent {
     for (uint32_t i = tid; i < (uint32_t)C::NB_MAX; i += C::NC) sm.bcnt[i] = 0u;
     if (tid < 8) sm.cls_cnt[tid] = 0u;
     if (tid == 0) sm.task_next = 0u;
-    constexpr int RS = C::SPLIT_SAMPLES / 32;  // samples per lane
-    constexpr int RUN = C::SPLIT_RUN;
-    constexpr int NRUN = C::SPLIT_SAMPLES / RUN;
+    // Pivots by rank: SPLIT_SAMPLES evenly spaced keys, each ranked by one thread against all of
+    // them (16-byte broadcast reads; equal keys ordered by index, so the ranks are a permutation).
+    // Pivot q is the sample of rank (q + 1) * step - 1; with q1 = q + 1 = (2p + 1) << (lg - l - 1)
+    // it is tree node 2^l + p.
     B* smp = sm.tileB;  // free until the scatter
-    if (warp == 0) {
-      B v[RS];
-#pragma unroll
-      for (int r = 0; r < RS; ++r)
-        v[r] = A[(uint32_t)(((unsigned long long)(r * 32 + lane) * m) / (unsigned long long)C::SPLIT_SAMPLES)];
-      // run lane / 4 holds its element (lane % 4) * RS + r in v[r]
-      warp_bitonic_n<RS, 1, B, RUN>(v);
-#pragma unroll
-      for (int r = 0; r < RS; ++r) smp[(uint32_t)lane * RS + r] = v[r];
-    }
+    if (tid < C::SPLIT_SAMPLES)
+      smp[tid] = A[(uint32_t)(((unsigned long long)tid * m) / (unsigned long long)C::SPLIT_SAMPLES)];
     cbar();
     if (tid < C::SPLIT_SAMPLES) {
-      // The rank of sample tid: its index in its run plus, in every other run, the samples that
-      // come before it (smaller ones, and equal ones of an earlier run). All searches are
-      // independent; the one in the sample's own run is made and discarded.
-      const uint32_t g = (uint32_t)tid / RUN, i = (uint32_t)tid % RUN;
       const B x = smp[tid];
       uint32_t rank = 0;
+      constexpr int PER16 = 16 / (int)sizeof(B);
+      const uint4* v4 = reinterpret_cast<const uint4*>(smp);
+#pragma unroll 4
+      for (int q = 0; q < C::SPLIT_SAMPLES / PER16; ++q) {
+        const uint4 w = v4[q];
+        B y[PER16];
+        memcpy(y, &w, 16);
 #pragma unroll
-      for (uint32_t h = 0; h < (uint32_t)NRUN; ++h) {
-        const B* run = smp + h * RUN;
-        uint32_t pos = 0;
-#pragma unroll
-        for (uint32_t st = RUN; st > 0; st >>= 1) {
-          if (pos + st <= (uint32_t)RUN) {
-            const B y = run[pos + st - 1];
-            if (h < g ? y <= x : y < x) pos += st;
-          }
-        }
-        rank += h == g ? i : pos;
+        for (int u = 0; u < PER16; ++u) rank += (y[u] < x) | ((y[u] == x) & (q * PER16 + u < tid));
       }
-      // pivot q is the sample of rank (q + 1) * step - 1; with q1 = q + 1 = (2p + 1) << (lg - l - 1)
-      // it is tree node 2^l + p
       const uint32_t step = (uint32_t)C::SPLIT_SAMPLES / nb;
       const uint32_t q1 = (rank + 1u) / step;
       if ((rank + 1u) % step == 0u && q1 < nb) {
