@@ -663,6 +663,8 @@ __global__ void __launch_bounds__(256) seed_kernel(SortArgs<typename C::T> a, co
                                                    unsigned long long n, uint32_t pairs, uint32_t from_dn) {
   const uint32_t seg = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
+  pdl_wait();     // the segment table and the zeroed queue are written by the work before it
+  pdl_trigger();  // the persistent kernel may launch; it waits for this grid before starting
   if (nseg_dev) {  // a replayable launch: the count is data, at most the launch's capacity
     const unsigned long long m = *nseg_dev;
     if (m > nseg) {
@@ -1902,6 +1904,7 @@ __global__ void __launch_bounds__(C::NT, min_blocks_per_sm<C>()) persistent_kern
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
+  pdl_wait();  // the seed kernel's jobs and tickets are visible from here on
 #ifdef GQS_PROFILE
   if (tid == 0) atomicCAS(&a.q->lvl_start, 0ull, (unsigned long long)global_timer_ns());
 #endif

@@ -48,6 +48,27 @@ struct LaunchParams {
   unsigned long long check_n;  // 0, or a tighter bound on key indices for -DGQS_CHECK builds' tests
 };
 
+// Launches `kernel`; with `early`, as a programmatic dependent launch: the grid may start while
+// the kernel before it in the stream finishes, and must call pdl_wait() before it reads anything
+// that kernel wrote. Only for a kernel whose predecessor in the stream is a kernel.
+template <class... KArgs, class... Args>
+inline cudaError_t launch_kernel(bool early, void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                                 cudaStream_t s, Args... args) {
+  cudaLaunchConfig_t cfg{};
+  cudaLaunchAttribute at[1];
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  if (early) {
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+  }
+  return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
 // Per key type (defined in gqs_sort_dispatch.cu).
 #define GQS_DECLARE_TYPE(S)                         \
   int variant_count_##S();                          \

@@ -105,6 +105,13 @@ __device__ __forceinline__ void sts_release(uint32_t* p, uint32_t v) {
   asm volatile("st.release.cta.shared.u32 [%0], %1;" ::"r"(smem_addr(p)), "r"(v) : "memory");
 }
 
+// ---- programmatic dependent launch ------------------------------------------
+// Waits until the grid launched before this one in the stream has completed and its writes are
+// visible. (Returns at once in a grid launched without programmatic stream serialization.)
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+// Lets the next grid in the stream begin launching; its pdl_wait still waits for this grid.
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 // ---- misc -------------------------------------------------------------------
 __device__ __forceinline__ uint64_t global_timer_ns() {
   uint64_t t;

@@ -41,10 +41,13 @@ using BOf = typename KeyOps<T>::B;
 
 template <class T>
 __global__ void __launch_bounds__(kThreads) split_pick(const BOf<T>* __restrict__ d, unsigned long long n, uint32_t k,
-                                                        uint32_t lg, uint32_t ns, BOf<T>* __restrict__ tree, Queue* q) {
+                                                        uint32_t lg, uint32_t ns, BOf<T>* __restrict__ tree,
+                                                        uint32_t* __restrict__ total, Queue* q) {
   using B = BOf<T>;
   __shared__ B smp[kMaxSamples];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  pdl_trigger();  // split_count may launch now; it waits for this grid before reading the tree
+  for (uint32_t i = tid; i < k; i += kThreads) total[i] = 0u;
 #ifdef GQS_PROFILE
   if (tid == 0) atomicCAS(&q->lvl_start, 0ull, (unsigned long long)global_timer_ns());  // per-level times start here
 #else
@@ -137,6 +140,8 @@ __global__ void __launch_bounds__(kThreads) split_count(const BOf<T>* __restrict
   using B = BOf<T>;
   __shared__ B t[kMaxK];
   __shared__ uint32_t cnt[kMaxK];
+  pdl_wait();
+  pdl_trigger();
   for (uint32_t i = threadIdx.x; i < k; i += kThreads) {
     t[i] = tree[i];
     cnt[i] = 0u;
@@ -164,6 +169,8 @@ __global__ void __launch_bounds__(kMaxK) split_starts(const uint32_t* __restrict
                                                       unsigned long long* __restrict__ segs, Queue* q) {
   __shared__ uint32_t wsum[32];
   const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  pdl_wait();
+  pdl_trigger();
   const uint32_t c = tid < k ? total[tid] : 0u;
   uint32_t inc = c;
 #pragma unroll
@@ -211,6 +218,8 @@ __global__ void __launch_bounds__(kThreads) split_scatter(const BOf<T>* __restri
   __shared__ B t[kMaxK];
   __shared__ uint32_t cur[kMaxK];
   __shared__ uint16_t lab[kMaxSlice];
+  pdl_wait();
+  pdl_trigger();
   for (uint32_t i = threadIdx.x; i < k; i += kThreads) {
     t[i] = tree[i];
     cur[i] = 0u;
@@ -265,14 +274,22 @@ cudaError_t launch_t(const SplitPlan& p, const void* d, void* dn, size_t n, void
   uint32_t* total = reinterpret_cast<uint32_t*>(base + kTreeBytes + kSegBytes);
   uint32_t* cursor = total + kMaxK;
   const B* src = static_cast<const B*>(d);
-  cudaError_t e = cudaMemsetAsync(total, 0, p.k * sizeof(uint32_t), s);
-  if (e != cudaSuccess) return e;
-  split_pick<T><<<1, kThreads, 0, s>>>(src, n, p.k, p.lg, p.samples, tree, q);
-  split_count<T><<<p.ctas, kThreads, 0, s>>>(src, n, p.k, p.lg, tree, total);
-  split_starts<<<1, kMaxK, 0, s>>>(total, p.k, n, cursor, sg, q);
-  split_scatter<T><<<p.ctas, kThreads, 0, s>>>(src, static_cast<B*>(dn), n, p.k, p.lg, tree, cursor);
+  // Each kernel after the first is a programmatic dependent launch of the one before (and the
+  // seed and persistent kernels follow the same way), so that each launches while the one
+  // before it drains; split_pick also zeroes the bucket totals.
+  split_pick<T><<<1, kThreads, 0, s>>>(src, n, p.k, p.lg, p.samples, tree, total, q);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess)
+    e = launch_kernel(true, split_count<T>, dim3(p.ctas), dim3(kThreads), 0, s, src, (unsigned long long)n, p.k, p.lg,
+                      (const B*)tree, total);
+  if (e == cudaSuccess)
+    e = launch_kernel(true, split_starts, dim3(1), dim3(kMaxK), 0, s, (const uint32_t*)total, p.k,
+                      (unsigned long long)n, cursor, sg, q);
+  if (e == cudaSuccess)
+    e = launch_kernel(true, split_scatter<T>, dim3(p.ctas), dim3(kThreads), 0, s, src, static_cast<B*>(dn),
+                      (unsigned long long)n, p.k, p.lg, (const B*)tree, cursor);
   *segs = sg;
-  return cudaGetLastError();
+  return e;
 }
 
 }  // namespace

@@ -45,12 +45,14 @@ struct VariantOps {
     a.n = p.check_n ? p.check_n : p.n;
     const uint32_t nseg = p.offsets ? p.nseg : 1u;
     const uint32_t seed_blocks = (nseg + 7u) / 8u;  // 8 warps per 256-thread block, one per segment
-    seed_kernel<C><<<seed_blocks, 256, 0, p.stream>>>(a, p.offsets, p.nseg_dev, nseg, p.n, p.pairs, p.from_dn);
-    cudaError_t e = cudaGetLastError();
+    // After a top split the seed kernel follows split_scatter as a programmatic dependent
+    // launch; the persistent kernel follows the seed kernel so whenever no event lies between.
+    cudaError_t e = launch_kernel(p.from_dn != 0, seed_kernel<C>, dim3(seed_blocks), dim3(256), 0, p.stream, a,
+                                  p.offsets, p.nseg_dev, nseg, (unsigned long long)p.n, p.pairs, p.from_dn);
     if (e != cudaSuccess) return e;
     if (p.ev_begin) cudaEventRecord(p.ev_begin, p.stream);
-    persistent_kernel<C><<<p.grid, C::NT, sizeof(Smem<C>), p.stream>>>(a);
-    e = cudaGetLastError();
+    e = launch_kernel(p.ev_begin == nullptr, persistent_kernel<C>, dim3(p.grid), dim3(C::NT), sizeof(Smem<C>),
+                      p.stream, a);
     if (p.ev_end) cudaEventRecord(p.ev_end, p.stream);
     return e;
   }
