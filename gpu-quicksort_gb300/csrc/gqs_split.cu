@@ -6,8 +6,8 @@
 // the children (about 11 us a level on a GB300), and 2^20 keys need seven levels before every
 // range fits one on-chip tile. The split replaces those levels with four short kernels over an
 // array that stays in L2:
-//   split_pick     one CTA: sorts 4 samples per bucket (runs of 256 by warp networks, then
-//                  ranks by binary search across runs) and keeps every 4th as a splitter, stored
+//   split_pick     one CTA: sorts 8 samples per bucket (runs of 256 by warp networks, then
+//                  merged pairwise by merge path) and keeps every 8th as a splitter, stored
 //                  as a breadth-first search tree (the on-chip split's layout and bucket rule:
 //                  bucket b holds splitter[b-1] < key <= splitter[b]);
 //   split_count    every CTA walks the tree for each key of its slice, counts per bucket in
@@ -33,18 +33,22 @@ constexpr int kThreads = 512;
 constexpr int kRun = 256;            // samples per warp-sorted run (8 per lane)
 constexpr uint32_t kMaxK = 1024;     // buckets
 constexpr uint32_t kMaxSamples = 4096;
-constexpr uint32_t kOversample = 4;  // samples per bucket
+constexpr uint32_t kOversample = 8;  // samples per bucket
 constexpr uint32_t kMaxSlice = 16384;  // keys of one CTA's slice in the scatter (labels in shared memory)
 
 template <class T>
 using BOf = typename KeyOps<T>::B;
+
+// Dynamic shared memory of split_pick: two sample buffers.
+extern __shared__ __align__(16) unsigned char split_dyn[];
 
 template <class T>
 __global__ void __launch_bounds__(kThreads) split_pick(const BOf<T>* __restrict__ d, unsigned long long n, uint32_t k,
                                                         uint32_t lg, uint32_t ns, BOf<T>* __restrict__ tree,
                                                         uint32_t* __restrict__ total, Queue* q) {
   using B = BOf<T>;
-  __shared__ B smp[kMaxSamples];
+  B* src = reinterpret_cast<B*>(split_dyn);
+  B* dst = src + kMaxSamples;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   pdl_trigger();  // split_count may launch now; it waits for this grid before reading the tree
   for (uint32_t i = tid; i < k; i += kThreads) total[i] = 0u;
@@ -63,34 +67,40 @@ __global__ void __launch_bounds__(kThreads) split_pick(const BOf<T>* __restrict_
     }
     warp_bitonic_n<8, 1, B>(v);  // element lane * 8 + r of the run
 #pragma unroll
-    for (int r = 0; r < 8; ++r) smp[warp * kRun + lane * 8 + r] = v[r];
+    for (int r = 0; r < 8; ++r) src[warp * kRun + lane * 8 + r] = v[r];
   }
   __syncthreads();
-  const uint32_t step = ns / k;
-  for (uint32_t i = tid; i < ns; i += kThreads) {
-    // rank among all samples: index in its run, plus the samples of every other run that come
-    // before it (smaller ones, and equal ones of an earlier run)
-    const uint32_t g = i / kRun;
-    const B x = smp[i];
-    uint32_t rank = i % kRun;
-    for (uint32_t h = 0; h < nrun; ++h) {
-      if (h == g) continue;
-      const B* run = smp + h * kRun;
-      uint32_t pos = 0;
-#pragma unroll
-      for (uint32_t st = kRun; st > 0; st >>= 1) {
-        if (pos + st <= (uint32_t)kRun) {
-          const B y = run[pos + st - 1];
-          if (h < g ? y <= x : y < x) pos += st;
-        }
+  // Merge the sorted runs pairwise until one run remains: each thread writes `per` consecutive
+  // outputs of one pair, starting where merge path puts its first output (the number of keys
+  // the first run contributes before it, by binary search on the diagonal).
+  const uint32_t per = ns / kThreads;  // ns is 256 << j; with ns >= 512, per divides every pair
+  for (uint32_t len = kRun; len < ns; len <<= 1) {
+    if (per > 0) {
+      const uint32_t o0 = (uint32_t)tid * per, base = o0 / (2u * len) * (2u * len), dg = o0 - base;
+      const B* x = src + base;
+      const B* y = x + len;
+      uint32_t lo = dg > len ? dg - len : 0u, hi = dg < len ? dg : len;
+      while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (x[mid] <= y[dg - 1u - mid]) lo = mid + 1u;
+        else hi = mid;
       }
-      rank += pos;
+      uint32_t i = lo, j = dg - lo;
+      for (uint32_t t = 0; t < per; ++t) {
+        const bool from_x = j >= len || (i < len && x[i] <= y[j]);
+        dst[o0 + t] = from_x ? x[i++] : y[j++];
+      }
     }
-    const uint32_t q1 = (rank + 1u) / step;  // splitter q1 - 1 is the sample of rank q1 * step - 1
-    if ((rank + 1u) % step == 0u && q1 < k) {
-      const uint32_t tz = (uint32_t)__ffs(q1) - 1u;
-      tree[(1u << (lg - 1u - tz)) + (q1 >> (tz + 1u))] = x;
-    }
+    __syncthreads();
+    B* const tmp = src;
+    src = dst;
+    dst = tmp;
+  }
+  // splitter q1 - 1 is the sample of rank q1 * step - 1
+  const uint32_t step = ns / k;
+  for (uint32_t q1 = (uint32_t)tid + 1u; q1 < k; q1 += kThreads) {
+    const uint32_t tz = (uint32_t)__ffs(q1) - 1u;
+    tree[(1u << (lg - 1u - tz)) + (q1 >> (tz + 1u))] = src[q1 * step - 1u];
   }
 }
 
@@ -274,10 +284,14 @@ cudaError_t launch_t(const SplitPlan& p, const void* d, void* dn, size_t n, void
   uint32_t* total = reinterpret_cast<uint32_t*>(base + kTreeBytes + kSegBytes);
   uint32_t* cursor = total + kMaxK;
   const B* src = static_cast<const B*>(d);
+  constexpr size_t kPickSmem = 2 * kMaxSamples * sizeof(B);
+  static const cudaError_t attr =
+      cudaFuncSetAttribute(split_pick<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kPickSmem);
+  if (attr != cudaSuccess) return attr;
   // Each kernel after the first is a programmatic dependent launch of the one before (and the
   // seed and persistent kernels follow the same way), so that each launches while the one
   // before it drains; split_pick also zeroes the bucket totals.
-  split_pick<T><<<1, kThreads, 0, s>>>(src, n, p.k, p.lg, p.samples, tree, total, q);
+  split_pick<T><<<1, kThreads, kPickSmem, s>>>(src, n, p.k, p.lg, p.samples, tree, total, q);
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess)
     e = launch_kernel(true, split_count<T>, dim3(p.ctas), dim3(kThreads), 0, s, src, (unsigned long long)n, p.k, p.lg,
